@@ -1,0 +1,316 @@
+#!/usr/bin/env python3
+"""Benchmark: bit-exact 2^27 x 2^27-limb three-prime NTT multiply on GB300.
+
+One step = one full product of two 2^27-limb operands (1 GiB each, uniform u64
+limbs from SplitMix64 seeds, top limb nonzero) through the library's nn_mul:
+forward transforms of both operands, pointwise product, inverse transform,
+CRT + carry into 2^28 product limbs.
+
+  value  device-resident: operands already in HBM, K steps timed with CUDA
+         events on the library's stream; product limbs/s over all ranks.
+  e2e    through the host-pointer API (nn_mul_host): pinned host operands
+         copied in, multiplied, the product copied back, every step.
+  roofline  the dominant kernel's algorithmic bytes per launch over its mean
+         event-timed duration, against the measured HBM copy bandwidth.
+  cpu_baseline  the oracle (CPU restatement of the reference, 1 thread) on a
+         bounded sample: one 2^24 x 2^24-limb product.
+
+Inputs (2 GiB operands, 6 GiB of residues per transform) are far larger than
+the 129 MB L2, so no flush is needed between steps.  Multi-GPU runs are
+independent replicas (weak scaling); `--impl reference` times the CPU path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "NTT-mul limbs/s (bit-exact) batched vs plain on GB300; % HBM roofline; p99"
+UNIT = "limbs/s"
+N_EXP = 27
+SEED_A, SEED_B = 1000 + (1 << N_EXP), 7777 + (1 << N_EXP)
+FALLBACK_HBM_GBS = 6800.0
+
+# Algorithmic bytes per launch of each kernel for a product of na x nb limbs
+# at transform length L (three primes, 8-byte residues):
+#   load+first pass reads the limbs once per prime and writes residues,
+#   a strided/contiguous pass reads and writes every residue once,
+#   pointwise reads two transforms and writes one, the CRT scan reads the
+#   residues and writes the product limbs.
+def kernel_bytes(name: str, na: int, nb: int, L: int) -> float:
+    if name == "ntt_fwd_load_pass":
+        return 4.0 * (na + nb) + 24.0 * L  # mean operand length: one launch per operand
+    if name in ("ntt_fwd_pass", "ntt_inv_pass", "ntt_inv_last_pass"):
+        return 48.0 * L
+    if name == "ntt_pointwise":
+        return 72.0 * L
+    if name == "crt_carry_scan":
+        return 24.0 * L + 8.0 * (na + nb)
+    return 0.0
+
+
+def mul_algorithmic_bytes(na: int, nb: int, L: int) -> float:
+    """16(na+nb) + 192 L: two load+column passes, two row passes (one fused
+    with the pointwise product and the inverse row pass), the inverse column
+    pass fused with CRT and carry."""
+    return 16.0 * (na + nb) + 192.0 * L
+
+
+def peaks() -> tuple[float, str]:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=10)
+
+    def summary(self) -> dict:
+        rows = []
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 9 and f[1].replace(".", "").isdigit():
+                    rows.append(f)
+        finally:
+            os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        busy = [x for x in sm if x >= 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(busy), "sm_max_mhz": float(rows[0][2]), "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit())}
+
+
+def cpu_baseline_port() -> dict:
+    """The oracle (single-threaded CPU restatement) on one 2^24 x 2^24 product."""
+    from natural_number_gb300.synth import limbs
+    from oracle import Oracle
+    n = 1 << 24
+    o = Oracle("port")
+    a, b = limbs(1, n), limbs(2, n)
+    t = o.time_mul(a, b, 1)
+    return {"value": 2 * n / t, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "one 2^24 x 2^24-limb product (2^27 workload scaled down 8x per operand), seconds=%.2f" % t}
+
+
+def _ref_worker(args):
+    n, seed = args
+    from natural_number_gb300.synth import limbs
+    from oracle import Oracle
+    o = Oracle("port")
+    a, b = limbs(seed, n), limbs(seed + 1, n)
+    t0 = time.perf_counter()
+    o.mul(a, b)
+    return time.perf_counter() - t0
+
+
+def run_reference(args) -> None:
+    """CPU reference arm: the oracle restatement (the reference's x86-64
+    assembly does not build on this Arm host), one independent product per
+    host core, so the whole CPU is used; each step is a bounded sample."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    from oracle import build_oracle
+    build_oracle()
+    cores = os.cpu_count() or 1
+    n = 1 << 22
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        for w in range(args.warmup):
+            pool.map(_ref_worker, [(n, 17 + 2 * i) for i in range(cores)])
+        t0 = time.perf_counter()
+        for s in range(args.steps):
+            pool.map(_ref_worker, [(n, 17 + 2 * i) for i in range(cores)])
+        dt = (time.perf_counter() - t0) / args.steps
+    value = cores * 2 * n / dt
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic (SplitMix64)",
+            "config": {"workload": "plain multiply, sampled: %d independent 2^22 x 2^22-limb products per step "
+                                   "(one per host core) standing in for one 2^27 x 2^27 product" % cores},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "%d x (2^22 x 2^22) per step" % cores},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n-exp", type=int, default=N_EXP, help="operand size 2^n limbs (27 = the benchmark workload)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import numpy as np
+    import torch
+
+    import natural_number_gb300 as nn
+    from natural_number_gb300.synth import limbs
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    n = 1 << args.n_exp
+    L = 1 << (args.n_exp + 1)
+    ctx = nn.Context(local)
+    stream = torch.cuda.current_stream()
+    a = limbs(SEED_A + rank, n)
+    b = limbs(SEED_B + rank, n)
+    da = torch.from_numpy(a).to("cuda")
+    db = torch.from_numpy(b).to("cuda")
+    out = torch.empty(2 * n, dtype=torch.uint64, device="cuda")
+
+    for _ in range(max(args.warmup, 3)):
+        ctx.mul_device(out, da, db)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = nn.launch_count()
+    nn.profile_enable(True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        start.record(stream)
+        for _ in range(args.steps):
+            ctx.mul_device(out, da, db)
+        stop.record(stream)
+        torch.cuda.synchronize()
+    nn.profile_enable(False)
+    prof = nn.profile_report()
+    launches = (nn.launch_count() - l0) / args.steps
+    ms = start.elapsed_time(stop) / args.steps
+    ctx.synchronize()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    value = world * 2 * n / (ms / 1e3)
+
+    # spot-check the last product with size-independent modular identities
+    prod = out.cpu().numpy()
+    from tests.gpu_util import mod_checks
+    ma, mb, mp = mod_checks(a), mod_checks(b), mod_checks(prod)
+    exact = mp[0] == ma[0] * mb[0] % (2**64 - 1) and mp[1] == ma[1] * mb[1] % (2**64 + 1)
+    del prod
+
+    e2e = None
+    if not args.no_e2e:
+        ha = torch.from_numpy(a).pin_memory().numpy()
+        hb = torch.from_numpy(b).pin_memory().numpy()
+        ho = torch.empty(2 * n, dtype=torch.uint64).pin_memory().numpy()
+        for _ in range(2):
+            ctx.mul(ha, hb, out=ho)
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            ctx.mul(ha, hb, out=ho)
+        e_ms = (time.perf_counter() - t0) / args.steps * 1e3
+        if dist:
+            t = torch.tensor([e_ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e_ms = float(t.item())
+        e2e = {"value": world * 2 * n / (e_ms / 1e3), "unit": UNIT, "ms_per_step": e_ms,
+               "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 16 * n}
+
+    if rank != 0:
+        return
+    peak, peak_kind = peaks()
+    dom = max(prof.items(), key=lambda kv: kv[1][1])
+    dname, (dcount, dms) = dom
+    d_avg = dms / dcount
+    d_bytes = kernel_bytes(dname, n, n, L)
+    achieved = d_bytes / (d_avg / 1e3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get(dname)
+        except Exception:
+            traffic = None
+    mul_bytes = mul_algorithmic_bytes(n, n, L)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic (SplitMix64 uniform u64 limbs, top limb nonzero)",
+        "config": {"workload": "plain multiply, 2^%d x 2^%d limbs (%d MiB per operand), product %d limbs"
+                               % (args.n_exp, args.n_exp, n * 8 >> 20, 2 * n),
+                   "l2": "inputs larger than L2 (operands %d MiB, residues %d MiB per transform); no flush"
+                         % (n * 8 >> 20, 24 * L >> 20),
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "bit_exact_spot_check": bool(exact)},
+        "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "bytes_per_launch": d_bytes, "launch_ms": d_avg, "launches_per_step": dcount / args.steps},
+        "mul_roofline": {"algorithmic_bytes": mul_bytes, "achieved": mul_bytes / (ms / 1e3) / 1e9,
+                         "frac": mul_bytes / (ms / 1e3) / 1e9 / peak},
+        "kernels": {k: {"launches_per_step": c / args.steps, "ms_per_step": t / args.steps} for k, (c, t) in prof.items()},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if e2e:
+        line["e2e"] = e2e
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline_port()
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,111 @@
+/* natural_gb300.h — C ABI of the GB300 big-number multiply path.
+ *
+ * Drop-in boundary for Natural_Number's multiply hot path: the three-prime
+ * NTT engine (struct NTT_info, ntt_info.h:10-67), the cached-transform helpers
+ * (natural.h:452-527) and the natural-level products, squares and quotients
+ * (natural.h:384-793).  Plain pointers and sizes only; limbs are little-endian
+ * uint64_t words as in basic_natural (basic_natural.h:9-13).
+ *
+ * Conventions
+ *  - Every call returns nn_status (the reference has no error returns and
+ *    exits on allocation failure, basic_natural.h:17-18).
+ *  - "d_" pointers are device pointers; device calls are ordered on the
+ *    context's stream and return before the GPU finishes.  "_host" calls take
+ *    host pointers, copy in, compute and copy out, and return when done.
+ *  - Sizes are limb counts.  Products of n_a and n_b limbs occupy n_a + n_b
+ *    limbs before normalisation (natural::std, natural.h:82-93).
+ *  - A context is used by one host thread at a time.
+ */
+#ifndef NATURAL_GB300_H
+#define NATURAL_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  NN_OK = 0,
+  NN_ERR_INVALID = 1,   /* argument outside the documented preconditions */
+  NN_ERR_OOM = 2,       /* device allocation failed */
+  NN_ERR_CUDA = 3,      /* CUDA runtime error; see nn_last_error */
+  NN_ERR_TIMEOUT = 4,   /* a bounded device-side wait gave up (carry lookback) */
+  NN_ERR_BUDGET = 5,    /* request exceeds the context's HBM budget */
+  NN_ERR_NO_DEVICE = 6  /* no CUDA device / kernels not loadable */
+} nn_status;
+
+typedef struct nn_context nn_context;
+typedef struct nn_transform nn_transform;
+
+/* ---- context ------------------------------------------------------------ */
+/* Creates a context on `device`.  hbm_budget_bytes = 0 means no budget. */
+nn_status nn_context_create(int device, uint64_t hbm_budget_bytes, nn_context** out);
+nn_status nn_context_destroy(nn_context* ctx);
+/* Use a caller-owned cudaStream_t (NULL restores the context's own stream). */
+nn_status nn_context_set_stream(nn_context* ctx, void* cuda_stream);
+void* nn_context_stream(nn_context* ctx);
+/* Waits for the stream and reports any deferred device-side error. */
+nn_status nn_context_synchronize(nn_context* ctx);
+const char* nn_status_string(nn_status s);
+const char* nn_last_error(const nn_context* ctx);
+/* Bytes of device memory the context holds (tables, transforms, scratch). */
+uint64_t nn_context_device_bytes(const nn_context* ctx);
+
+/* ---- NTT_info: device-resident transforms (ntt_info.h:10-67) ------------- */
+nn_status nn_transform_create(nn_context* ctx, nn_transform** out);
+nn_status nn_transform_destroy(nn_context* ctx, nn_transform* t);
+/* NTT_info::NTT_scale; 0 after a base-case "save" (natural.h:453-456). */
+int nn_transform_scale(const nn_transform* t);
+void nn_transform_set_scale(nn_transform* t, int scale);
+/* NTT_info::load (ntt_info.h:147-173) fused with NTT_info::NTT
+ * (ntt_info.h:180-198): residues of n <= 2^scale limbs under the three primes,
+ * transformed.  Grows the twiddle tables as NTT_info::init does (ntt_info.h:22-41). */
+nn_status nn_transform_forward(nn_context* ctx, nn_transform* t, const uint64_t* d_limbs, uint64_t n, int scale);
+/* NTT_info::mul (ntt_info.h:224-231): dst = a (.) b; dst may be a or b. */
+nn_status nn_transform_pointwise(nn_context* ctx, nn_transform* dst, const nn_transform* a, const nn_transform* b);
+/* NTT_info::INTT (ntt_info.h:200-221) followed by NTT_info::save
+ * (ntt_info.h:237-248): writes `size` limbs, or, when size-1 > 2^scale (wrap
+ * mode), the product mod B^(2^scale) - 1 in 2^scale limbs.  The transform's
+ * residues are consumed.  *written (host) receives the limb count written. */
+nn_status nn_transform_inverse_save(nn_context* ctx, nn_transform* t, uint64_t* d_out, uint64_t size,
+                                    uint64_t* written);
+/* Copies the 3 x 2^scale residues (prime-major) to d_out (inspection/testing). */
+nn_status nn_transform_residues(nn_context* ctx, const nn_transform* t, uint64_t* d_out);
+
+/* ---- products on device pointers ---------------------------------------- */
+/* natural::_mul (natural.h:444-450): base case below 384 limbs, NTT above,
+ * with the unbalanced split of natural.h:391-419.  d_out: n_a + n_b limbs. */
+nn_status nn_mul(nn_context* ctx, uint64_t* d_out, const uint64_t* d_a, uint64_t n_a, const uint64_t* d_b,
+                 uint64_t n_b);
+/* natural::_sqr (natural.h:529-535).  d_out: 2 n limbs. */
+nn_status nn_sqr(nn_context* ctx, uint64_t* d_out, const uint64_t* d_a, uint64_t n);
+/* The load/NTT/mul/INTT/save pipeline at a caller-chosen scale, as
+ * _mul_NTT runs it (natural.h:399-405); size-1 > 2^scale selects wrap mode.
+ * n_a, n_b <= 2^scale.  d_out: max(size, 2^scale) limbs; *written as above. */
+nn_status nn_ntt_mul(nn_context* ctx, uint64_t* d_out, const uint64_t* d_a, uint64_t n_a, const uint64_t* d_b,
+                     uint64_t n_b, int scale, uint64_t size, uint64_t* written);
+/* Schoolbook product (asmMul1 / mul_base, base.h:56-81) on the GPU: n_a+n_b limbs. */
+nn_status nn_mul_base(nn_context* ctx, uint64_t* d_out, const uint64_t* d_a, uint64_t n_a, const uint64_t* d_b,
+                      uint64_t n_b);
+
+/* ---- launch accounting (process-wide) ------------------------------------ */
+/* Number of kernels this library has launched since load. */
+uint64_t nn_launch_count(void);
+/* Bracket every launch with CUDA events (off by default). */
+void nn_profile_enable(int on);
+/* Writes "kernel count total_ms" lines for the launches recorded since the
+ * last report (synchronises on their events) into buf; returns the length. */
+uint64_t nn_profile_report(char* buf, uint64_t cap);
+
+/* ---- host-pointer entry points (copy in, compute, copy out) ------------- */
+/* *out_n receives the normalised limb count; out holds n_a + n_b limbs. */
+nn_status nn_mul_host(nn_context* ctx, uint64_t* out, uint64_t* out_n, const uint64_t* a, uint64_t n_a,
+                      const uint64_t* b, uint64_t n_b);
+nn_status nn_sqr_host(nn_context* ctx, uint64_t* out, uint64_t* out_n, const uint64_t* a, uint64_t n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NATURAL_GB300_H */

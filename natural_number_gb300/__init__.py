@@ -1,0 +1,255 @@
+"""GB300-native big-number multiply path (Natural_Number's three-prime NTT
+multiply, base case, Newton division) — Python access to the C ABI.
+
+The compute lives in libnatural_gb300.so (sm_103a CUDA kernels + C++ host
+orchestration, include/natural_gb300.h).  This module is a thin ctypes layer
+for tests, benchmarks and Python callers; it has no CPU fallback: if the
+library or a CUDA device is missing, calls raise.
+
+Host-pointer calls take and return numpy uint64 arrays (little-endian limbs,
+like basic_natural).  Device calls take torch uint64 CUDA tensors and are
+ordered on the context's stream (set to torch's current stream by default).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+LIB_PATH = os.path.join(HERE, "_build", "libnatural_gb300.so")
+HEADER = os.path.join(ROOT, "include", "natural_gb300.h")
+
+NN_OK, NN_ERR_INVALID, NN_ERR_OOM, NN_ERR_CUDA, NN_ERR_TIMEOUT, NN_ERR_BUDGET, NN_ERR_NO_DEVICE = range(7)
+
+_u64p = C.POINTER(C.c_uint64)
+_vp = C.c_void_p
+_lib = None
+
+
+class NNError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{msg} (status {status})")
+        self.status = status
+
+
+def header_functions() -> list[str]:
+    """Names of every function declared in include/natural_gb300.h."""
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:[\w\s\*]+?)\b(nn_\w+)\s*\(", txt, flags=re.M)))
+
+
+def lib() -> C.CDLL:
+    """Loads the extension (building it first when nvcc is available)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        from . import build as _b
+        _b.build()
+    L = C.CDLL(LIB_PATH)
+    sig = {
+        "nn_context_create": (C.c_int, [C.c_int, C.c_uint64, C.POINTER(_vp)]),
+        "nn_context_destroy": (C.c_int, [_vp]),
+        "nn_context_set_stream": (C.c_int, [_vp, _vp]),
+        "nn_context_stream": (_vp, [_vp]),
+        "nn_context_synchronize": (C.c_int, [_vp]),
+        "nn_status_string": (C.c_char_p, [C.c_int]),
+        "nn_last_error": (C.c_char_p, [_vp]),
+        "nn_context_device_bytes": (C.c_uint64, [_vp]),
+        "nn_transform_create": (C.c_int, [_vp, C.POINTER(_vp)]),
+        "nn_transform_destroy": (C.c_int, [_vp, _vp]),
+        "nn_transform_scale": (C.c_int, [_vp]),
+        "nn_transform_set_scale": (None, [_vp, C.c_int]),
+        "nn_transform_forward": (C.c_int, [_vp, _vp, _vp, C.c_uint64, C.c_int]),
+        "nn_transform_pointwise": (C.c_int, [_vp, _vp, _vp, _vp]),
+        "nn_transform_inverse_save": (C.c_int, [_vp, _vp, _vp, C.c_uint64, _u64p]),
+        "nn_transform_residues": (C.c_int, [_vp, _vp, _vp]),
+        "nn_mul": (C.c_int, [_vp, _vp, _vp, C.c_uint64, _vp, C.c_uint64]),
+        "nn_sqr": (C.c_int, [_vp, _vp, _vp, C.c_uint64]),
+        "nn_ntt_mul": (C.c_int, [_vp, _vp, _vp, C.c_uint64, _vp, C.c_uint64, C.c_int, C.c_uint64, _u64p]),
+        "nn_mul_base": (C.c_int, [_vp, _vp, _vp, C.c_uint64, _vp, C.c_uint64]),
+        "nn_launch_count": (C.c_uint64, []),
+        "nn_profile_enable": (None, [C.c_int]),
+        "nn_profile_report": (C.c_uint64, [C.c_char_p, C.c_uint64]),
+        "nn_mul_host": (C.c_int, [_vp, _u64p, _u64p, _u64p, C.c_uint64, _u64p, C.c_uint64]),
+        "nn_sqr_host": (C.c_int, [_vp, _u64p, _u64p, _u64p, C.c_uint64]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _np(x) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(x, dtype=np.uint64))
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(_u64p)
+
+
+def _dptr(t) -> int:
+    """Device pointer of a torch CUDA tensor (uint64 limbs)."""
+    if not t.is_cuda:
+        raise ValueError("expected a CUDA tensor")
+    return t.data_ptr()
+
+
+class Context:
+    """nn_context: one CUDA device, one stream, twiddle tables and scratch."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0, use_torch_stream: bool = True):
+        L = lib()
+        h = _vp()
+        st = L.nn_context_create(device, hbm_budget, C.byref(h))
+        if st != NN_OK:
+            raise NNError(st, "nn_context_create: " + L.nn_status_string(st).decode())
+        self.h = h
+        self.device = device
+        if use_torch_stream:
+            try:
+                import torch
+                if torch.cuda.is_available():
+                    self.set_stream(torch.cuda.current_stream(device).cuda_stream)
+            except ImportError:
+                pass
+
+    # -- plumbing -------------------------------------------------------------
+    def _check(self, st: int, what: str) -> None:
+        if st != NN_OK:
+            msg = lib().nn_last_error(self.h).decode()
+            raise NNError(st, f"{what}: {lib().nn_status_string(st).decode()}: {msg}")
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            lib().nn_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        self._check(lib().nn_context_set_stream(self.h, _vp(stream_ptr or 0)), "set_stream")
+
+    def synchronize(self) -> None:
+        self._check(lib().nn_context_synchronize(self.h), "synchronize")
+
+    def device_bytes(self) -> int:
+        return lib().nn_context_device_bytes(self.h)
+
+    # -- host-pointer API (natural.h operator surface) ------------------------
+    def mul(self, a, b, out: np.ndarray | None = None) -> np.ndarray:
+        """natural operator* on host arrays; `out` (n_a + n_b limbs, e.g. pinned) is reused if given."""
+        a, b = _np(a), _np(b)
+        if out is None:
+            out = np.empty(a.size + b.size, dtype=np.uint64)
+        elif out.dtype != np.uint64 or out.size < a.size + b.size or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous uint64 array of n_a + n_b limbs")
+        n = C.c_uint64()
+        self._check(lib().nn_mul_host(self.h, _ptr(out), C.byref(n), _ptr(a), a.size, _ptr(b), b.size), "mul")
+        return out[: n.value]
+
+    def sqr(self, a, out: np.ndarray | None = None) -> np.ndarray:
+        a = _np(a)
+        if out is None:
+            out = np.empty(2 * a.size, dtype=np.uint64)
+        elif out.dtype != np.uint64 or out.size < 2 * a.size or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous uint64 array of 2 n limbs")
+        n = C.c_uint64()
+        self._check(lib().nn_sqr_host(self.h, _ptr(out), C.byref(n), _ptr(a), a.size), "sqr")
+        return out[: n.value]
+
+    # -- device-pointer API ---------------------------------------------------
+    def mul_device(self, out, a, b, na: int | None = None, nb: int | None = None) -> None:
+        na = a.numel() if na is None else na
+        nb = b.numel() if nb is None else nb
+        self._check(lib().nn_mul(self.h, _vp(_dptr(out)), _vp(_dptr(a)), na, _vp(_dptr(b)), nb), "nn_mul")
+
+    def sqr_device(self, out, a, n: int | None = None) -> None:
+        n = a.numel() if n is None else n
+        self._check(lib().nn_sqr(self.h, _vp(_dptr(out)), _vp(_dptr(a)), n), "nn_sqr")
+
+    def mul_base_device(self, out, a, b) -> None:
+        self._check(lib().nn_mul_base(self.h, _vp(_dptr(out)), _vp(_dptr(a)), a.numel(), _vp(_dptr(b)), b.numel()),
+                    "nn_mul_base")
+
+    def ntt_mul_device(self, out, a, b, scale: int, size: int) -> int:
+        w = C.c_uint64()
+        self._check(lib().nn_ntt_mul(self.h, _vp(_dptr(out)), _vp(_dptr(a)), a.numel(), _vp(_dptr(b)), b.numel(),
+                                     scale, size, C.byref(w)), "nn_ntt_mul")
+        return w.value
+
+    def transform(self) -> "Transform":
+        return Transform(self)
+
+
+class Transform:
+    """nn_transform — the device-resident NTT_info (ntt_info.h:10-67)."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        h = _vp()
+        ctx._check(lib().nn_transform_create(ctx.h, C.byref(h)), "transform_create")
+        self.h = h
+
+    @property
+    def scale(self) -> int:
+        return lib().nn_transform_scale(self.h)
+
+    def forward(self, limbs, scale: int, n: int | None = None) -> "Transform":
+        n = limbs.numel() if n is None else n
+        self.ctx._check(lib().nn_transform_forward(self.ctx.h, self.h, _vp(_dptr(limbs)), n, scale), "forward")
+        return self
+
+    def pointwise(self, a: "Transform", b: "Transform") -> "Transform":
+        self.ctx._check(lib().nn_transform_pointwise(self.ctx.h, self.h, a.h, b.h), "pointwise")
+        return self
+
+    def inverse_save(self, out, size: int) -> int:
+        w = C.c_uint64()
+        self.ctx._check(lib().nn_transform_inverse_save(self.ctx.h, self.h, _vp(_dptr(out)), size, C.byref(w)),
+                        "inverse_save")
+        return w.value
+
+    def residues(self, out) -> None:
+        self.ctx._check(lib().nn_transform_residues(self.ctx.h, self.h, _vp(_dptr(out))), "residues")
+
+    def close(self) -> None:
+        if getattr(self, "h", None) and self.ctx.h:
+            lib().nn_transform_destroy(self.ctx.h, self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def launch_count() -> int:
+    """Kernels launched by the library so far (process-wide)."""
+    return int(lib().nn_launch_count())
+
+
+def profile_enable(on: bool) -> None:
+    lib().nn_profile_enable(int(bool(on)))
+
+
+def profile_report() -> dict:
+    """{kernel: (launches, total_ms)} for launches recorded since the last report."""
+    buf = C.create_string_buffer(1 << 20)  # the report consumes the records: read once
+    lib().nn_profile_report(buf, len(buf))
+    out = {}
+    for line in buf.value.decode().splitlines():
+        name, cnt, ms = line.split()
+        out[name] = (int(cnt), float(ms))
+    return out

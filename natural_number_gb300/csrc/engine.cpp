@@ -1,0 +1,418 @@
+// engine.cpp — context, device-resident transforms and the C ABI of
+// include/natural_gb300.h.  Host C++ that orders the sm_103a kernels of
+// ntt.cu / carry.cu on one CUDA stream; no computation happens on the host
+// besides size bookkeeping and the final normalisation of host results.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <bit>
+#include <cstring>
+#include <string>
+
+#include "../../include/natural_gb300.h"
+#include "nn_internal.h"
+
+using nn::u64;
+
+namespace {
+constexpr u64 kNttMulThreshold = 384;  // ntt_info.h:6
+
+int ntt_scale(u64 n1, u64 n2) {  // get_NTT_scale (natural.h:384-386)
+  u64 v = n1 + n2 - 2;
+  return 64 - std::countl_zero(v);
+}
+}  // namespace
+
+struct nn_context {
+  int device = 0;
+  cudaStream_t own = nullptr;
+  cudaStream_t stream = nullptr;
+  u64 budget = 0;
+  u64 held = 0;  // bytes of live allocations made through the context
+  nn::Tables tables;
+  nn::Scan scan;
+  std::string err;
+};
+
+struct nn_transform {
+  u64* res = nullptr;  // [3][2^scale]
+  u64 words = 0;       // allocated words (3 * 2^scale at most)
+  int scale = 0;
+};
+
+namespace {
+
+nn_status fail(nn_context* c, cudaError_t e, const char* what) {
+  c->err = std::string(what) + ": " + cudaGetErrorString(e);
+  cudaGetLastError();  // clear sticky-free errors
+  return e == cudaErrorMemoryAllocation ? NN_ERR_OOM : NN_ERR_CUDA;
+}
+
+#define NN_CK(ctx, expr, what)                           \
+  do {                                                   \
+    cudaError_t _e = (expr);                             \
+    if (_e != cudaSuccess) return fail((ctx), _e, what); \
+  } while (0)
+
+nn_status dev_alloc(nn_context* c, u64** p, u64 words) {
+  const u64 bytes = std::max<u64>(words, 1) * sizeof(u64);
+  if (c->budget && c->held + bytes > c->budget) {
+    c->err = "HBM budget exceeded";
+    return NN_ERR_BUDGET;
+  }
+  cudaError_t e = cudaMallocAsync((void**)p, bytes, c->stream);
+  if (e != cudaSuccess) return fail(c, e, "cudaMallocAsync");
+  c->held += bytes;
+  return NN_OK;
+}
+
+void dev_free(nn_context* c, u64* p, u64 words) {
+  if (!p) return;
+  cudaFreeAsync(p, c->stream);
+  c->held -= std::max<u64>(words, 1) * sizeof(u64);
+}
+
+// RAII device buffer tied to the context's stream.
+struct DBuf {
+  nn_context* c;
+  u64* p = nullptr;
+  u64 words = 0;
+  explicit DBuf(nn_context* ctx) : c(ctx) {}
+  nn_status alloc(u64 w) {
+    words = w;
+    return dev_alloc(c, &p, w);
+  }
+  ~DBuf() { dev_free(c, p, words); }
+};
+
+nn_status xform_reserve(nn_context* c, nn_transform* t, int s) {
+  const u64 need = 3ull << s;
+  if (t->words < need) {
+    dev_free(c, t->res, t->words);
+    t->res = nullptr;
+    t->words = 0;
+    nn_status st = dev_alloc(c, &t->res, need);
+    if (st != NN_OK) return st;
+    t->words = need;
+  }
+  t->scale = s;
+  return NN_OK;
+}
+
+nn_status forward(nn_context* c, nn_transform* t, const u64* d_limbs, u64 n, int s) {
+  if (s < 2 || s > 40 || n == 0 || n > (1ull << s)) {
+    c->err = "forward: need 2 <= scale <= 40 and 1 <= n <= 2^scale";
+    return NN_ERR_INVALID;
+  }
+  NN_CK(c, nn::tables_ensure(c->tables, s, c->stream), "twiddle tables");
+  nn_status st = xform_reserve(c, t, s);
+  if (st != NN_OK) return st;
+  NN_CK(c, nn::ntt_forward(d_limbs, n, t->res, s, c->tables, c->stream), "forward NTT");
+  return NN_OK;
+}
+
+nn_status inverse_save(nn_context* c, nn_transform* t, u64* d_out, u64 size, u64* written) {
+  if (size < 2) {
+    c->err = "save: size must be at least 2";
+    return NN_ERR_INVALID;
+  }
+  NN_CK(c, nn::ntt_inverse(t->res, t->scale, c->tables, c->stream), "inverse NTT");
+  u64 w = 0;
+  NN_CK(c, nn::ntt_save(t->res, t->scale, d_out, size, c->scan, &w, c->stream), "CRT/carry");
+  if (written) *written = w;
+  return NN_OK;
+}
+
+nn_status pointwise(nn_context* c, nn_transform* dst, const nn_transform* a, const nn_transform* b) {
+  if (a->scale != b->scale || a->scale < 2) {
+    c->err = "pointwise: transforms differ in scale";
+    return NN_ERR_INVALID;
+  }
+  nn_status st = xform_reserve(c, dst, a->scale);
+  if (st != NN_OK) return st;
+  NN_CK(c, nn::ntt_pointwise(dst->res, a->res, b->res, a->scale, c->tables, c->stream), "pointwise");
+  return NN_OK;
+}
+
+// Balanced NTT product at scale s into d_out (size limbs, or wrap).
+nn_status ntt_product(nn_context* c, u64* d_out, const u64* a, u64 na, const u64* b, u64 nb, int s, u64 size,
+                      u64* written) {
+  nn_transform xa, xb;
+  nn_status st = forward(c, &xa, a, na, s);
+  if (st == NN_OK) st = forward(c, &xb, b, nb, s);
+  if (st == NN_OK) st = pointwise(c, &xb, &xa, &xb);
+  if (st == NN_OK) st = inverse_save(c, &xb, d_out, size, written);
+  dev_free(c, xa.res, xa.words);
+  dev_free(c, xb.res, xb.words);
+  return st;
+}
+
+nn_status mul_impl(nn_context* c, u64* d_out, const u64* a, u64 na, const u64* b, u64 nb) {
+  if (!d_out || !a || !b || na == 0 || nb == 0) {
+    c->err = "mul: null pointer or empty operand";
+    return NN_ERR_INVALID;
+  }
+  if (na < nb) {
+    std::swap(a, b);
+    std::swap(na, nb);
+  }
+  if (nb < kNttMulThreshold) {  // natural.h:445-446 -> _mul_base
+    NN_CK(c, nn::school_mul(a, na, b, nb, d_out, c->scan, c->stream), "base-case product");
+    return NN_OK;
+  }
+  // natural::_mul_NTT (natural.h:391-419)
+  const u64 a0 = (na + 1) >> 1;
+  const int s = ntt_scale(na, nb), s_opt = ntt_scale(a0, nb);
+  if (s == s_opt) return ntt_product(c, d_out, a, na, b, nb, s, na + nb, nullptr);
+  // Unbalanced: b's transform is made once at s_opt and reused for both
+  // halves of a (mul_save_NTT_info / mul_load_NTT_info, natural.h:452-515).
+  const u64 a1 = na - a0;
+  nn_transform xb, x0, x1;
+  DBuf p0(c), p1(c);
+  nn_status st = p0.alloc(a0 + nb);
+  if (st == NN_OK) st = p1.alloc(a1 + nb);
+  if (st == NN_OK) st = forward(c, &xb, b, nb, s_opt);
+  if (st == NN_OK) st = forward(c, &x0, a, a0, s_opt);
+  if (st == NN_OK) st = pointwise(c, &x0, &xb, &x0);
+  if (st == NN_OK) st = inverse_save(c, &x0, p0.p, a0 + nb, nullptr);
+  if (st == NN_OK) st = forward(c, &x1, a + a0, a1, s_opt);
+  if (st == NN_OK) st = pointwise(c, &x1, &xb, &x1);
+  if (st == NN_OK) st = inverse_save(c, &x1, p1.p, a1 + nb, nullptr);
+  // (a1*b << a0 limbs) + a0*b  (natural.h:417)
+  if (st == NN_OK) {
+    cudaError_t e = nn::add_shifted(p0.p, a0 + nb, p1.p, a1 + nb, a0, d_out, na + nb, c->scan, c->stream);
+    if (e != cudaSuccess) st = fail(c, e, "split combine");
+  }
+  dev_free(c, xb.res, xb.words);
+  dev_free(c, x0.res, x0.words);
+  dev_free(c, x1.res, x1.words);
+  return st;
+}
+
+nn_status sqr_impl(nn_context* c, u64* d_out, const u64* a, u64 n) {
+  if (!d_out || !a || n == 0) {
+    c->err = "sqr: null pointer or empty operand";
+    return NN_ERR_INVALID;
+  }
+  if (n < kNttMulThreshold) {  // natural.h:530-531 -> _sqr_base
+    NN_CK(c, nn::school_mul(a, n, a, n, d_out, c->scan, c->stream), "base-case square");
+    return NN_OK;
+  }
+  // natural::_sqr_NTT (natural.h:433-442): one transform, squared pointwise.
+  const int s = ntt_scale(n, n);
+  nn_transform x;
+  nn_status st = forward(c, &x, a, n, s);
+  if (st == NN_OK) st = pointwise(c, &x, &x, &x);
+  if (st == NN_OK) st = inverse_save(c, &x, d_out, 2 * n, nullptr);
+  dev_free(c, x.res, x.words);
+  return st;
+}
+
+u64 normalized(const u64* x, u64 n) {  // natural::std (natural.h:82-93)
+  while (n > 1 && x[n - 1] == 0) --n;
+  return n;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* nn_status_string(nn_status s) {
+  switch (s) {
+    case NN_OK: return "ok";
+    case NN_ERR_INVALID: return "invalid argument";
+    case NN_ERR_OOM: return "device out of memory";
+    case NN_ERR_CUDA: return "CUDA error";
+    case NN_ERR_TIMEOUT: return "device wait timed out";
+    case NN_ERR_BUDGET: return "HBM budget exceeded";
+    case NN_ERR_NO_DEVICE: return "no CUDA device";
+  }
+  return "unknown";
+}
+
+uint64_t nn_launch_count(void) { return nn::launch_count(); }
+
+void nn_profile_enable(int on) { nn::profile_enable(on != 0); }
+
+uint64_t nn_profile_report(char* buf, uint64_t cap) {
+  std::string r = nn::profile_report();
+  if (buf && cap) {
+    u64 n = std::min<u64>(cap - 1, r.size());
+    std::memcpy(buf, r.data(), n);
+    buf[n] = 0;
+  }
+  return r.size();
+}
+
+nn_status nn_context_create(int device, uint64_t budget, nn_context** out) {
+  if (!out) return NN_ERR_INVALID;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count <= device || device < 0) {
+    cudaGetLastError();
+    return NN_ERR_NO_DEVICE;
+  }
+  nn_context* c = new nn_context;
+  c->device = device;
+  c->budget = budget;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = nn::upload_primes();
+  if (e == cudaSuccess) {
+    cudaMemPool_t pool;
+    e = cudaDeviceGetDefaultMemPool(&pool, device);
+    if (e == cudaSuccess) {
+      uint64_t keep = ~0ull;  // keep freed blocks cached for reuse
+      e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+  }
+  if (e == cudaSuccess) e = nn::scan_reserve(c->scan, 1024);
+  if (e != cudaSuccess) {
+    nn_status st = e == cudaErrorNoDevice || e == cudaErrorNoKernelImageForDevice ? NN_ERR_NO_DEVICE : NN_ERR_CUDA;
+    cudaGetLastError();
+    if (c->own) cudaStreamDestroy(c->own);
+    delete c;
+    return st;
+  }
+  c->stream = c->own;
+  *out = c;
+  return NN_OK;
+}
+
+nn_status nn_context_destroy(nn_context* c) {
+  if (!c) return NN_ERR_INVALID;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  nn::tables_free(c->tables);
+  nn::scan_free(c->scan);
+  if (c->own) cudaStreamDestroy(c->own);
+  delete c;
+  return NN_OK;
+}
+
+nn_status nn_context_set_stream(nn_context* c, void* s) {
+  if (!c) return NN_ERR_INVALID;
+  c->stream = s ? (cudaStream_t)s : c->own;
+  return NN_OK;
+}
+
+void* nn_context_stream(nn_context* c) { return c ? (void*)c->stream : nullptr; }
+
+nn_status nn_context_synchronize(nn_context* c) {
+  if (!c) return NN_ERR_INVALID;
+  NN_CK(c, cudaStreamSynchronize(c->stream), "synchronize");
+  nn::u32 err = 0;
+  NN_CK(c, cudaMemcpy(&err, c->scan.err, sizeof err, cudaMemcpyDeviceToHost), "read error flag");
+  if (err) {
+    cudaMemset(c->scan.err, 0, sizeof err);
+    c->err = "carry lookback wait exceeded its bound";
+    return NN_ERR_TIMEOUT;
+  }
+  return NN_OK;
+}
+
+const char* nn_last_error(const nn_context* c) { return c ? c->err.c_str() : "no context"; }
+
+uint64_t nn_context_device_bytes(const nn_context* c) {
+  if (!c) return 0;
+  return c->held + 2 * 3 * c->tables.cap * sizeof(u64) + (c->scan.max_tiles + 1) * 4;
+}
+
+nn_status nn_transform_create(nn_context* c, nn_transform** out) {
+  if (!c || !out) return NN_ERR_INVALID;
+  *out = new nn_transform;
+  return NN_OK;
+}
+
+nn_status nn_transform_destroy(nn_context* c, nn_transform* t) {
+  if (!c || !t) return NN_ERR_INVALID;
+  dev_free(c, t->res, t->words);
+  delete t;
+  return NN_OK;
+}
+
+int nn_transform_scale(const nn_transform* t) { return t ? t->scale : 0; }
+void nn_transform_set_scale(nn_transform* t, int s) {
+  if (t) t->scale = s;
+}
+
+nn_status nn_transform_forward(nn_context* c, nn_transform* t, const uint64_t* d, uint64_t n, int s) {
+  if (!c || !t || !d) return NN_ERR_INVALID;
+  return forward(c, t, d, n, s);
+}
+
+nn_status nn_transform_pointwise(nn_context* c, nn_transform* dst, const nn_transform* a, const nn_transform* b) {
+  if (!c || !dst || !a || !b || !a->res || !b->res) return NN_ERR_INVALID;
+  return pointwise(c, dst, a, b);
+}
+
+nn_status nn_transform_inverse_save(nn_context* c, nn_transform* t, uint64_t* d_out, uint64_t size,
+                                    uint64_t* written) {
+  if (!c || !t || !t->res || !d_out) return NN_ERR_INVALID;
+  return inverse_save(c, t, d_out, size, written);
+}
+
+nn_status nn_transform_residues(nn_context* c, const nn_transform* t, uint64_t* d_out) {
+  if (!c || !t || !t->res || !d_out) return NN_ERR_INVALID;
+  NN_CK(c, cudaMemcpyAsync(d_out, t->res, (3ull << t->scale) * sizeof(u64), cudaMemcpyDeviceToDevice, c->stream),
+        "copy residues");
+  return NN_OK;
+}
+
+nn_status nn_mul(nn_context* c, uint64_t* d_out, const uint64_t* a, uint64_t na, const uint64_t* b, uint64_t nb) {
+  if (!c) return NN_ERR_INVALID;
+  return mul_impl(c, d_out, a, na, b, nb);
+}
+
+nn_status nn_sqr(nn_context* c, uint64_t* d_out, const uint64_t* a, uint64_t n) {
+  if (!c) return NN_ERR_INVALID;
+  return sqr_impl(c, d_out, a, n);
+}
+
+nn_status nn_ntt_mul(nn_context* c, uint64_t* d_out, const uint64_t* a, uint64_t na, const uint64_t* b, uint64_t nb,
+                     int s, uint64_t size, uint64_t* written) {
+  if (!c || !d_out || !a || !b) return NN_ERR_INVALID;
+  return ntt_product(c, d_out, a, na, b, nb, s, size, written);
+}
+
+nn_status nn_mul_base(nn_context* c, uint64_t* d_out, const uint64_t* a, uint64_t na, const uint64_t* b,
+                      uint64_t nb) {
+  if (!c || !d_out || !a || !b || !na || !nb) return NN_ERR_INVALID;
+  NN_CK(c, nn::school_mul(a, na, b, nb, d_out, c->scan, c->stream), "base-case product");
+  return NN_OK;
+}
+
+nn_status nn_mul_host(nn_context* c, uint64_t* out, uint64_t* out_n, const uint64_t* a, uint64_t na,
+                      const uint64_t* b, uint64_t nb) {
+  if (!c || !out || !a || !b || !na || !nb) return NN_ERR_INVALID;
+  DBuf da(c), db(c), dout(c);
+  nn_status st = da.alloc(na);
+  if (st == NN_OK) st = db.alloc(nb);
+  if (st == NN_OK) st = dout.alloc(na + nb);
+  if (st != NN_OK) return st;
+  NN_CK(c, cudaMemcpyAsync(da.p, a, na * 8, cudaMemcpyHostToDevice, c->stream), "H2D");
+  NN_CK(c, cudaMemcpyAsync(db.p, b, nb * 8, cudaMemcpyHostToDevice, c->stream), "H2D");
+  st = mul_impl(c, dout.p, da.p, na, db.p, nb);
+  if (st != NN_OK) return st;
+  NN_CK(c, cudaMemcpyAsync(out, dout.p, (na + nb) * 8, cudaMemcpyDeviceToHost, c->stream), "D2H");
+  st = nn_context_synchronize(c);
+  if (st == NN_OK && out_n) *out_n = normalized(out, na + nb);
+  return st;
+}
+
+nn_status nn_sqr_host(nn_context* c, uint64_t* out, uint64_t* out_n, const uint64_t* a, uint64_t n) {
+  if (!c || !out || !a || !n) return NN_ERR_INVALID;
+  DBuf da(c), dout(c);
+  nn_status st = da.alloc(n);
+  if (st == NN_OK) st = dout.alloc(2 * n);
+  if (st != NN_OK) return st;
+  NN_CK(c, cudaMemcpyAsync(da.p, a, n * 8, cudaMemcpyHostToDevice, c->stream), "H2D");
+  st = sqr_impl(c, dout.p, da.p, n);
+  if (st != NN_OK) return st;
+  NN_CK(c, cudaMemcpyAsync(out, dout.p, 2 * n * 8, cudaMemcpyDeviceToHost, c->stream), "D2H");
+  st = nn_context_synchronize(c);
+  if (st == NN_OK && out_n) *out_n = normalized(out, 2 * n);
+  return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,81 @@
+// nn_internal.h — device-side building blocks shared by the engine.
+// Host C++; no CUDA types leak past this header except cudaStream_t/cudaError_t.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace nn {
+
+typedef std::uint64_t u64;
+typedef unsigned int u32;
+
+// Host copy of the prime constants; uploaded to __constant__ memory once per device.
+void primes_host(u64 p[3]);
+cudaError_t upload_primes();
+
+// Twiddle tables in the reference's layout (ntt_info.h:22-41): per prime,
+// words 2k and 2k+1 hold w_k = prod_{bit t of k} root_base[t+1] and its Shoup
+// companion floor(w_k * 2^64 / p) + 1.  Grow-only; a table built for scale s
+// serves every smaller scale.
+struct Tables {
+  u64* root = nullptr;   // [3][cap] forward
+  u64* iroot = nullptr;  // [3][cap] inverse
+  u64 cap = 0;           // words per prime (= 2^(scale-1))
+  int scale = 0;
+};
+cudaError_t tables_ensure(Tables& t, int s, cudaStream_t st);
+void tables_free(Tables& t);
+
+// One tiled pass over transform levels [lambda0, lambda0 + R) with C columns per tile.
+struct Pass {
+  int lambda0, R, C;
+};
+std::vector<Pass> plan_passes(int s);
+
+// Scratch for the decoupled-lookback carry scan.
+struct Scan {
+  u32* flags = nullptr;  // per-tile status words
+  u32* counter = nullptr;
+  u32* err = nullptr;    // nonzero after a lookback wait gave up
+  u64* side = nullptr;   // limbs of the scan beyond the output (the carry words)
+  u64 max_tiles = 0;
+};
+constexpr int kScanThreads = 256;
+constexpr int kScanE = 8;  // limbs per thread
+constexpr u64 kScanTile = (u64)kScanThreads * kScanE;
+
+// Forward transform: limbs (n <= 2^s) -> residues [3][2^s], raw values in
+// [0,2p) identical to NTT_info::load + NTT (ntt_info.h:147-198).
+cudaError_t ntt_forward(const u64* limbs, u64 n, u64* res, int s, const Tables& t, cudaStream_t st);
+// Pointwise product of degree-1 residues (ntt_info.h:224-231); dst may alias a or b.
+cudaError_t ntt_pointwise(u64* dst, const u64* a, const u64* b, int s, const Tables& t, cudaStream_t st);
+// Inverse transform with the final 2^-(s-1) scale (ntt_info.h:200-221); values in [0,p).
+cudaError_t ntt_inverse(u64* res, int s, const Tables& t, cudaStream_t st);
+// CRT + carry into `size` limbs (normal mode) or the wrapped product mod
+// B^L - 1 in L limbs when size-1 > L (ntt_info.h:237-248).  Returns the
+// number of limbs written through *written (host value).
+cudaError_t ntt_save(const u64* res, int s, u64* out, u64 size, Scan& sc, u64* written, cudaStream_t st);
+// Schoolbook product by column sums + carry scan: out[0..na+nb).
+cudaError_t school_mul(const u64* a, u64 na, const u64* b, u64 nb, u64* out, Scan& sc, cudaStream_t st);
+// out[0..n) = x (nx limbs) + y (ny limbs) shifted up by `shift` limbs; the
+// carry out of limb n-1 is dropped.  out must not alias x or y (a tile
+// re-reads the inputs just below it while its predecessor may be writing).
+cudaError_t add_shifted(const u64* x, u64 nx, const u64* y, u64 ny, u64 shift, u64* out, u64 n, Scan& sc,
+                        cudaStream_t st);
+
+// Launch accounting (profile.cpp): every launch site brackets its kernel.
+void launch_begin(const char* name, cudaStream_t st);
+void launch_end(cudaStream_t st);
+unsigned long long launch_count();
+void profile_enable(bool on);
+std::string profile_report();
+
+u64 scan_tiles(u64 positions);
+cudaError_t scan_reserve(Scan& sc, u64 tiles);
+void scan_free(Scan& sc);
+
+}  // namespace nn

@@ -1,0 +1,384 @@
+// ntt.cu — three-prime NTT on sm_103a: twiddle tables, tiled forward/inverse
+// passes and the pointwise product.
+//
+// The transform is the reference's CRT-tree decomposition (ntt_info.h:180-221):
+// level lambda (0 <= lambda <= s-2) splits each block of 2^(s-lambda) words into
+// halves x, y and applies (x, y) -> (x + w y, x - w y) with w = root[2b] for
+// block b.  Level 0 is the load's radix-2 stage (ntt_info.h:153-171, twiddle
+// 1); the last level (pairs) is folded into the pointwise product.  Because
+// every butterfly reduces exactly, the residues after each level are
+// bit-identical to the reference's, whatever the grouping of levels.
+//
+// GPU mapping: levels are grouped into passes.  A pass over levels
+// [lambda0, lambda0+R) sees, inside each block of 2^(s-lambda0) words, S = 2^(s-
+// lambda0-R) interleaved columns of 2^R rows (row stride S).  A CTA stages
+// C columns x 2^R rows of one prime in shared memory with coalesced row
+// segments, runs the R levels as radix-8/4/2 register units (twiddles read
+// as 16-byte (w, w') pairs through the read-only cache), and writes the tile
+// back.  The first forward pass reads limbs and reduces them on the fly; the
+// last inverse pass applies the 2^-(s-1) scale on the way out.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "nn_device.cuh"
+#include "nn_internal.h"
+
+namespace nn {
+
+NN_DEFINE_PRIME_UPLOADER(upload_primes_ntt)
+
+namespace {
+
+typedef unsigned __int128 h128;
+
+const u64 kCoef[3] = {27, 58, 87};
+const u64 kGen[3] = {11, 2, 310};  // primitive 2^56-th roots; root_base[i][j] = g^(2^(55-j))
+
+u64 h_mulmod(u64 a, u64 b, u64 p) { return (u64)((h128)a * b % p); }
+u64 h_pow(u64 b, u64 e, u64 p) {
+  u64 r = 1;
+  for (; e; e >>= 1, b = h_mulmod(b, b, p))
+    if (e & 1) r = h_mulmod(r, b, p);
+  return r;
+}
+u64 h_comp(u64 w, u64 p) { return (u64)(((h128)w << 64) / p) + 1; }
+
+PrimeSet make_primes() {
+  PrimeSet ps{};
+  for (int i = 0; i < 3; ++i) {
+    u64 p = kCoef[i] << 56 | 1;
+    ps.p[i] = p;
+    ps.m64[i] = (u64)(~(u64)0 / p) + 1;
+    ps.mu[i] = (u64)(((h128)1 << (124 + i)) / p);
+    ps.c_hi[i] = (u32)(kCoef[i] << 24);
+  }
+  const u64 p0 = ps.p[0], p1 = ps.p[1], p2 = ps.p[2];
+  ps.inv01 = h_pow(p0 % p1, p1 - 2, p1);
+  ps.inv01s = h_comp(ps.inv01, p1);
+  ps.inv02 = h_pow(p0 % p2, p2 - 2, p2);
+  ps.inv02s = h_comp(ps.inv02, p2);
+  ps.inv12 = h_pow(p1 % p2, p2 - 2, p2);
+  ps.inv12s = h_comp(ps.inv12, p2);
+  h128 p01 = (h128)p0 * p1;
+  ps.p01_lo = (u64)p01;
+  ps.p01_hi = (u64)(p01 >> 64);
+  return ps;
+}
+
+// ---------------------------------------------------------------------------
+// Twiddle tables
+// ---------------------------------------------------------------------------
+
+// Extends one prime's table from n to 2n words: entry n+2k is entry 2k times
+// root_base[j] (ntt_info.h:29-31), followed by its Shoup companion.  The
+// companion floor(w*2^64/p)+1 uses V = floor((2^128-1)/p): q0 = floor(w*V/2^64)
+// is floor(w*2^64/p) or one less, decided by the remainder w*2^64 - q0*p < 2p.
+__global__ void twiddle_extend_kernel(u64* tab, u64 n, u64 bw, u64 bwp, int prime, u64 v_hi, u64 v_lo) {
+  u64 k = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (2 * k >= n) return;
+  const u64 p = g_primes.p[prime];
+  const u32 ch = g_primes.c_hi[prime];
+  u64 w = shoup_mul(tab[2 * k], bw, bwp, p, ch);
+  u64 q0 = mulhi(w, v_lo) + w * v_hi;
+  u64 r = (u64)0 - mul_p(q0, ch);
+  if (r >= p) ++q0;
+  tab[n + 2 * k] = w;
+  tab[n + 2 * k + 1] = q0 + 1;
+}
+
+// ---------------------------------------------------------------------------
+// Tiled passes
+// ---------------------------------------------------------------------------
+
+template <int K, int C, bool INV>
+__device__ __forceinline__ void level_group(u64* sm, int l, int R, u64 ksb, const u64* __restrict__ tw, u64 p,
+                                            u32 ch) {
+  const int nsub = R - l - K;
+  const int units = C << (R - K);
+  for (int u = threadIdx.x; u < units; u += blockDim.x) {
+    const int i = u & (C - 1);
+    const int v = u / C;
+    const int t0 = v & ((1 << nsub) - 1);
+    const int rb = v >> nsub;
+    const int row0 = (rb << (R - l)) + t0;
+    const int rstep = 1 << nsub;
+    const u64 bidx = (ksb << l) + (u64)rb;
+    u64 x[1 << K];
+#pragma unroll
+    for (int m = 0; m < (1 << K); ++m) x[m] = sm[(row0 + m * rstep) * C + i];
+    if (!INV) {
+#pragma unroll
+      for (int lv = 0; lv < K; ++lv) {
+        const int half = (1 << K) >> (lv + 1);
+#pragma unroll
+        for (int g = 0; g < (1 << lv); ++g) {
+          const ulonglong2 wv = __ldg(reinterpret_cast<const ulonglong2*>(tw) + ((bidx << lv) + g));
+#pragma unroll
+          for (int m = 0; m < half; ++m) fwd_bfly(x[g * 2 * half + m], x[g * 2 * half + m + half], wv.x, wv.y, p, ch);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int lv = K - 1; lv >= 0; --lv) {
+        const int half = (1 << K) >> (lv + 1);
+#pragma unroll
+        for (int g = 0; g < (1 << lv); ++g) {
+          const ulonglong2 wv = __ldg(reinterpret_cast<const ulonglong2*>(tw) + ((bidx << lv) + g));
+#pragma unroll
+          for (int m = 0; m < half; ++m) inv_bfly(x[g * 2 * half + m], x[g * 2 * half + m + half], wv.x, wv.y, p, ch);
+        }
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < (1 << K); ++m) sm[(row0 + m * rstep) * C + i] = x[m];
+  }
+}
+
+// FIRST: input is limbs (n_in of them, zero beyond); otherwise residues [3][L].
+// SCALE: multiply by 2^-(s-1) on the way out (last inverse pass).
+template <int C, bool FIRST, bool INV, bool SCALE>
+__global__ void __launch_bounds__(256) ntt_pass_kernel(const u64* in, u64* out, u64 n_in, int s, int lambda0, int R,
+                                                       const u64* __restrict__ tab, u64 tab_stride) {
+  extern __shared__ u64 sm[];
+  const int prime = blockIdx.y;
+  const u64 p = g_primes.p[prime];
+  const u32 ch = g_primes.c_hi[prime];
+  const u64 L = 1ull << s;
+  const u64* tw = tab + (u64)prime * tab_stride;
+  const int lg_s = s - lambda0 - R;
+  const u64 tiles_per_sb = (1ull << lg_s) / C;
+  const u64 tile = blockIdx.x;
+  const u64 ksb = tile / tiles_per_sb;
+  const u64 base = (ksb << (lg_s + R)) + (tile % tiles_per_sb) * C;
+  const int nel = C << R;
+
+  if (FIRST) {
+    const u64 m64 = g_primes.m64[prime];
+    for (int idx = threadIdx.x; idx < nel; idx += blockDim.x) {
+      const u64 pos = base + ((u64)(idx / C) << lg_s) + (idx & (C - 1));
+      sm[idx] = pos < n_in ? limb_mod(in[pos], m64, p, ch) : 0;
+    }
+  } else {
+    const u64* src = in + (u64)prime * L;
+    for (int idx = 2 * threadIdx.x; idx < nel; idx += 2 * blockDim.x) {
+      const u64 pos = base + ((u64)(idx / C) << lg_s) + (idx & (C - 1));
+      const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(src + pos);
+      sm[idx] = v.x;
+      sm[idx + 1] = v.y;
+    }
+  }
+  __syncthreads();
+
+  if (!INV) {
+    for (int l = 0; l < R;) {
+      const int k = R - l >= 3 ? 3 : R - l;
+      if (k == 3)
+        level_group<3, C, false>(sm, l, R, ksb, tw, p, ch);
+      else if (k == 2)
+        level_group<2, C, false>(sm, l, R, ksb, tw, p, ch);
+      else
+        level_group<1, C, false>(sm, l, R, ksb, tw, p, ch);
+      __syncthreads();
+      l += k;
+    }
+  } else {
+    for (int l = R; l > 0;) {
+      const int k = l >= 3 ? 3 : l;
+      l -= k;
+      if (k == 3)
+        level_group<3, C, true>(sm, l, R, ksb, tw, p, ch);
+      else if (k == 2)
+        level_group<2, C, true>(sm, l, R, ksb, tw, p, ch);
+      else
+        level_group<1, C, true>(sm, l, R, ksb, tw, p, ch);
+      __syncthreads();
+    }
+  }
+
+  u64* dst = out + (u64)prime * L;
+  for (int idx = 2 * threadIdx.x; idx < nel; idx += 2 * blockDim.x) {
+    const u64 pos = base + ((u64)(idx / C) << lg_s) + (idx & (C - 1));
+    ulonglong2 v = make_ulonglong2(sm[idx], sm[idx + 1]);
+    if (SCALE) {
+      v.x = div_pow2(v.x, (u32)(s - 1), p);
+      v.y = div_pow2(v.y, (u32)(s - 1), p);
+    }
+    *reinterpret_cast<ulonglong2*>(dst + pos) = v;
+  }
+}
+
+// Pointwise product of the degree-1 residues (a0 + a1 x)(b0 + b1 x) mod
+// (x^2 - w) and (a2 + a3 x)(b2 + b3 x) mod (x^2 + w), w = root[2g]
+// (ntt_info.h:224-231, asmLinux.asm:910-1057).  Inputs in [0,2p), outputs in [0,p).
+__global__ void __launch_bounds__(256) pointwise_kernel(u64* dst, const u64* a, const u64* b, u64 L,
+                                                        const u64* __restrict__ tab, u64 tab_stride) {
+  const int i = blockIdx.y;
+  const u64 g = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= L / 4) return;
+  const u64 p = g_primes.p[i];
+  const u32 ch = g_primes.c_hi[i];
+  const ulonglong2 wv = __ldg(reinterpret_cast<const ulonglong2*>(tab + (u64)i * tab_stride) + g);
+  const ulonglong2* A = reinterpret_cast<const ulonglong2*>(a + (u64)i * L) + 2 * g;
+  const ulonglong2* B = reinterpret_cast<const ulonglong2*>(b + (u64)i * L) + 2 * g;
+  ulonglong2 A0 = A[0], A1 = A[1], B0 = B[0], B1 = B[1];
+  const u64 a0 = reduce2p(A0.x, p), a1 = reduce2p(A0.y, p), a2 = reduce2p(A1.x, p), a3 = reduce2p(A1.y, p);
+  const u64 b0 = reduce2p(B0.x, p), b1 = reduce2p(B0.y, p), b2 = reduce2p(B1.x, p), b3 = reduce2p(B1.y, p);
+  const u64 wb1 = shoup_mul(b1, wv.x, wv.y, p, ch);
+  const u64 wb3 = shoup_mul(b3, wv.x, wv.y, p, ch);
+  const u64 nwb3 = wb3 ? p - wb3 : 0;
+  ulonglong2 R0, R1;
+  R0.x = barrett(add128(mul_wide(a0, b0), mul_wide(a1, wb1)), i);
+  R0.y = barrett(add128(mul_wide(a0, b1), mul_wide(a1, b0)), i);
+  R1.x = barrett(add128(mul_wide(a2, b2), mul_wide(a3, nwb3)), i);
+  R1.y = barrett(add128(mul_wide(a2, b3), mul_wide(a3, b2)), i);
+  ulonglong2* D = reinterpret_cast<ulonglong2*>(dst + (u64)i * L) + 2 * g;
+  D[0] = R0;
+  D[1] = R1;
+}
+
+template <int C, bool FIRST, bool INV, bool SCALE>
+cudaError_t launch_pass(const u64* in, u64* out, u64 n_in, int s, const Pass& ps, const Tables& t, cudaStream_t st) {
+  const size_t smem = (size_t)ps.C << ps.R << 3;
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(ntt_pass_kernel<C, FIRST, INV, SCALE>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  const u64 tiles = (1ull << s) / ((u64)ps.C << ps.R);
+  dim3 grid((unsigned)tiles, 3);
+  launch_begin(FIRST ? "ntt_fwd_load_pass" : INV ? (SCALE ? "ntt_inv_last_pass" : "ntt_inv_pass") : "ntt_fwd_pass", st);
+  ntt_pass_kernel<C, FIRST, INV, SCALE><<<grid, 256, smem, st>>>(in, out, n_in, s, ps.lambda0, ps.R,
+                                                                  INV ? t.iroot : t.root, t.cap);
+  launch_end(st);
+  return cudaGetLastError();
+}
+
+template <bool FIRST, bool INV, bool SCALE>
+cudaError_t dispatch_pass(const u64* in, u64* out, u64 n_in, int s, const Pass& ps, const Tables& t, cudaStream_t st) {
+  if (ps.C == 16) return launch_pass<16, FIRST, INV, SCALE>(in, out, n_in, s, ps, t, st);
+  return launch_pass<2, FIRST, INV, SCALE>(in, out, n_in, s, ps, t, st);
+}
+
+}  // namespace
+
+void primes_host(u64 p[3]) {
+  for (int i = 0; i < 3; ++i) p[i] = kCoef[i] << 56 | 1;
+}
+
+cudaError_t upload_primes() {
+  PrimeSet ps = make_primes();
+  cudaError_t e = upload_primes_ntt(ps);
+  return e == cudaSuccess ? upload_primes_carry(ps) : e;
+}
+
+cudaError_t tables_ensure(Tables& t, int s, cudaStream_t st) {
+  if (s < 2) s = 2;
+  const u64 need = 1ull << (s - 1);
+  if (t.cap >= need) return cudaSuccess;
+  u64 *root = nullptr, *iroot = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&root, 3 * need * sizeof(u64), st);
+  if (e != cudaSuccess) return e;
+  e = cudaMallocAsync((void**)&iroot, 3 * need * sizeof(u64), st);
+  if (e != cudaSuccess) {
+    cudaFreeAsync(root, st);
+    return e;
+  }
+  u64 have = t.cap;
+  for (int i = 0; i < 3; ++i) {
+    const u64 p = kCoef[i] << 56 | 1;
+    if (have) {
+      cudaMemcpyAsync(root + i * need, t.root + i * have, have * sizeof(u64), cudaMemcpyDeviceToDevice, st);
+      cudaMemcpyAsync(iroot + i * need, t.iroot + i * have, have * sizeof(u64), cudaMemcpyDeviceToDevice, st);
+    } else {
+      const u64 init[2] = {1, h_comp(1, p)};  // ntt_info.h:141-143
+      cudaMemcpyAsync(root + i * need, init, sizeof init, cudaMemcpyHostToDevice, st);
+      cudaMemcpyAsync(iroot + i * need, init, sizeof init, cudaMemcpyHostToDevice, st);
+    }
+  }
+  const u64 start = have ? have : 2;
+  for (int i = 0; i < 3; ++i) {
+    const u64 p = kCoef[i] << 56 | 1;
+    const h128 V = (~(h128)0) / p;
+    const u64 v_hi = (u64)(V >> 64), v_lo = (u64)V;
+    const u64 g = kGen[i], gi = h_pow(g, p - 2, p);
+    for (u64 n = start; n < need; n <<= 1) {
+      int j = 63 - __builtin_clzll(n);  // root_base index for this level
+      u64 bw = h_pow(g, 1ull << (55 - j), p), bwi = h_pow(gi, 1ull << (55 - j), p);
+      unsigned blocks = (unsigned)((n / 2 + 255) / 256);
+      launch_begin("twiddle_extend", st);
+      twiddle_extend_kernel<<<blocks, 256, 0, st>>>(root + i * need, n, bw, h_comp(bw, p), i, v_hi, v_lo);
+      launch_end(st);
+      launch_begin("twiddle_extend", st);
+      twiddle_extend_kernel<<<blocks, 256, 0, st>>>(iroot + i * need, n, bwi, h_comp(bwi, p), i, v_hi, v_lo);
+      launch_end(st);
+    }
+  }
+  e = cudaGetLastError();
+  if (t.root) cudaFreeAsync(t.root, st);
+  if (t.iroot) cudaFreeAsync(t.iroot, st);
+  t.root = root;
+  t.iroot = iroot;
+  t.cap = need;
+  t.scale = s;
+  return e;
+}
+
+void tables_free(Tables& t) {
+  if (t.root) cudaFree(t.root);
+  if (t.iroot) cudaFree(t.iroot);
+  t = Tables{};
+}
+
+std::vector<Pass> plan_passes(int s) {
+  // Levels 0..s-2.  The deepest pass works on contiguous blocks (C = 2 columns
+  // of stride 2) of up to 2^12 words; the levels above it go in strided
+  // passes of at most 9 levels with 16-column (128-byte) row segments.
+  std::vector<Pass> out;
+  const int total = s - 1;
+  const int r_last = std::min(total, 11);
+  int rest = total - r_last;
+  const int n_mid = (rest + 8) / 9;
+  int l = 0;
+  for (int k = 0; k < n_mid; ++k) {
+    int r = rest / (n_mid - k);
+    out.push_back(Pass{l, r, 16});
+    l += r;
+    rest -= r;
+  }
+  out.push_back(Pass{l, r_last, 2});
+  return out;
+}
+
+cudaError_t ntt_forward(const u64* limbs, u64 n, u64* res, int s, const Tables& t, cudaStream_t st) {
+  std::vector<Pass> plan = plan_passes(s);
+  for (size_t k = 0; k < plan.size(); ++k) {
+    cudaError_t e = k == 0 ? dispatch_pass<true, false, false>(limbs, res, n, s, plan[k], t, st)
+                           : dispatch_pass<false, false, false>(res, res, 0, s, plan[k], t, st);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t ntt_inverse(u64* res, int s, const Tables& t, cudaStream_t st) {
+  std::vector<Pass> plan = plan_passes(s);
+  for (size_t k = plan.size(); k-- > 0;) {
+    cudaError_t e = k == 0 ? dispatch_pass<false, true, true>(res, res, 0, s, plan[k], t, st)
+                           : dispatch_pass<false, true, false>(res, res, 0, s, plan[k], t, st);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t ntt_pointwise(u64* dst, const u64* a, const u64* b, int s, const Tables& t, cudaStream_t st) {
+  const u64 groups = (1ull << s) / 4;
+  dim3 grid((unsigned)((groups + 255) / 256), 3);
+  launch_begin("ntt_pointwise", st);
+  pointwise_kernel<<<grid, 256, 0, st>>>(dst, a, b, 1ull << s, t.root, t.cap);
+  launch_end(st);
+  return cudaGetLastError();
+}
+
+}  // namespace nn

@@ -1,0 +1,150 @@
+"""GPU parity: the sm_103a NTT path against the oracle and the reference's
+golden vectors, through the C ABI.  Integer work, so every check is bit-exact."""
+import numpy as np
+import pytest
+
+from gpu_util import P, digest, empty_dev, mod_checks, normalize, to_dev, to_host
+from natural_number_gb300.synth import limbs
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import natural_number_gb300 as nn
+    c = nn.Context(0)
+    yield c
+    c.close()
+
+
+@pytest.mark.parametrize("s,n", [(3, 2), (3, 4), (4, 7), (10, 300), (10, 1000), (12, 2048), (12, 3000),
+                                 (14, 16384), (15, 9000), (21, 1 << 20), (21, (1 << 20) + 12345), (23, 3 << 21)])
+def test_forward_residues_bit_identical(ctx, oracle, s, n):
+    """Residues after load + forward NTT equal the oracle's raw values exactly
+    (same CRT-tree order, same lazy [0,2p) representation)."""
+    a = limbs(1000 + s * 7 + n, n)
+    t = ctx.transform().forward(to_dev(a), s)
+    out = empty_dev(3 << s)
+    t.residues(out)
+    got = to_host(out).reshape(3, 1 << s)
+    want = oracle.ntt_forward(a, s)
+    for i in range(3):
+        if not np.array_equal(got[i], want[i]):
+            bad = np.nonzero(got[i] != want[i])[0]
+            pytest.fail(f"prime {i}: {bad.size} mismatches, first at {bad[:5]}")
+
+
+def test_forward_golden_canonical(ctx, golden):
+    for c in golden["ntt_forward"]:
+        s = c["scale"]
+        t = ctx.transform().forward(to_dev(limbs(c["seed"], c["n"])), s)
+        out = empty_dev(3 << s)
+        t.residues(out)
+        got = to_host(out).reshape(3, 1 << s)
+        assert digest(got.ravel()) == c["raw"]
+        canon = np.stack([got[i] % np.uint64(P[i]) for i in range(3)])
+        assert digest(canon.ravel()) == c["canonical"]
+
+
+def test_ntt_raw_golden_including_wrap(ctx, golden):
+    for c in golden["ntt_raw"]:
+        a, b = limbs(c["seed_a"], c["na"]), limbs(c["seed_b"], c["nb"])
+        s, size = c["scale"], c["size"]
+        out = empty_dev(max(size, 1 << s))
+        w = ctx.ntt_mul_device(out, to_dev(a), to_dev(b), s, size)
+        assert w == c["out"]["n"]
+        assert digest(to_host(out, w)) == c["out"], c
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_ntt_raw_random_wrap_vs_oracle(ctx, oracle, seed):
+    rng = np.random.default_rng(seed)
+    s = int(rng.integers(9, 15))
+    L = 1 << s
+    na = int(rng.integers(L // 3, L + 1))
+    nb = int(rng.integers(L // 3, L + 1))
+    size = int(rng.choice([na + nb, L + 1, L + 2, L + 7, na + nb + 5]))
+    a, b = limbs(seed * 31 + 1, na), limbs(seed * 31 + 2, nb)
+    if seed % 2:  # saturated limbs stress the carry chain
+        a[:] = np.uint64(2**64 - 1)
+        b[: nb // 2] = np.uint64(2**64 - 1)
+    out = empty_dev(max(size, L))
+    w = ctx.ntt_mul_device(out, to_dev(a), to_dev(b), s, size)
+    want = oracle.ntt_mul_raw(a, b, s, size)
+    assert w == want.size
+    assert np.array_equal(to_host(out, w), want)
+
+
+def test_mul_golden(ctx, golden):
+    for c in golden["mul"]:
+        a, b = limbs(c["seed_a"], c["na"]), limbs(c["seed_b"], c["nb"])
+        assert digest(ctx.mul(a, b)) == c["out"], (c["na"], c["nb"])
+
+
+def test_sqr_golden(ctx, golden):
+    for c in golden["sqr"]:
+        assert digest(ctx.sqr(limbs(c["seed"], c["n"]))) == c["out"], c["n"]
+
+
+@pytest.mark.parametrize("na,nb", [(1, 1), (1, 5), (7, 1), (31, 33), (383, 5000), (384, 384), (385, 4000),
+                                   (1000, 999), (4097, 4095), (70001, 65536), (100000, 50001), (262145, 131072)])
+def test_mul_vs_oracle(ctx, oracle, na, nb):
+    a, b = limbs(na * 3 + 1, na), limbs(nb * 5 + 2, nb)
+    assert np.array_equal(ctx.mul(a, b), oracle.mul(a, b))
+
+
+def test_mul_edge_values(ctx, oracle):
+    cases = [([0], [0]), ([0], list(range(1, 600))), ([2**64 - 1] * 500, [2**64 - 1] * 700),
+             ([1], [2**64 - 1] * 3), ([0, 0, 1], [0, 1]), ([2**64 - 1] * 4096, [2**64 - 1] * 4096)]
+    for a, b in cases:
+        a = np.array(a, dtype=np.uint64)
+        b = np.array(b, dtype=np.uint64)
+        assert np.array_equal(normalize(ctx.mul(a, b)), normalize(oracle.mul(a, b)))
+    for n in (1, 47, 383, 384, 5000):
+        a = np.full(n, 2**64 - 1, dtype=np.uint64)
+        assert np.array_equal(ctx.sqr(a), oracle.sqr(a))
+
+
+def test_device_api_matches_host_api(ctx, oracle):
+    a, b = limbs(11, 50000), limbs(12, 30000)
+    out = empty_dev(80000)
+    ctx.mul_device(out, to_dev(a), to_dev(b))
+    assert np.array_equal(normalize(to_host(out)), oracle.mul(a, b))
+    out2 = empty_dev(100000)
+    ctx.sqr_device(out2, to_dev(a))
+    assert np.array_equal(normalize(to_host(out2)), oracle.sqr(a))
+
+
+def test_config1_plain_multiply_bit_exact(ctx, oracle):
+    """2^20 x 2^20 limbs, seeded, against the oracle's operator*."""
+    n = 1 << 20
+    a, b = limbs(1, n), limbs(2, n)
+    got = ctx.mul(a, b)
+    assert got.size == 2 * n
+    assert np.array_equal(got, oracle.mul(a, b))
+
+
+def test_config2_large_multiply_and_square(ctx, golden):
+    """2^27-limb operands: digest of the reference's own product/square when
+    the big fixtures exist, plus size-independent modular checks."""
+    n = 1 << 27
+    a, b = limbs(1000 + n, n), limbs(7777 + n, n)
+    da, db = to_dev(a), to_dev(b)
+    out = empty_dev(2 * n)
+    ctx.mul_device(out, da, db)
+    prod = to_host(out)
+    ma, mb, mp = mod_checks(a), mod_checks(b), mod_checks(prod)
+    assert mp[0] == ma[0] * mb[0] % (2**64 - 1)
+    assert mp[1] == ma[1] * mb[1] % (2**64 + 1)
+    for c in golden.get("big_mul", []):
+        if c["na"] == n:
+            assert digest(normalize(prod)) == c["out"]
+    del prod
+    ctx.sqr_device(out, da)
+    sq = to_host(out)
+    ms = mod_checks(sq)
+    assert ms[0] == ma[0] * ma[0] % (2**64 - 1)
+    assert ms[1] == ma[1] * ma[1] % (2**64 + 1)
+    for c in golden.get("big_sqr", []):
+        if c["n"] == n:
+            assert digest(normalize(sq)) == c["out"]
