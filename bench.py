@@ -46,9 +46,9 @@ FALLBACK_HBM_GBS = 6800.0
 #   pointwise reads two transforms and writes one, the CRT scan reads the
 #   residues and writes the product limbs.
 def kernel_bytes(name: str, na: int, nb: int, L: int) -> float:
-    if name == "ntt_fwd_load_pass":
+    if name.startswith("ntt_fwd_load"):
         return 4.0 * (na + nb) + 24.0 * L  # mean operand length: one launch per operand
-    if name in ("ntt_fwd_pass", "ntt_inv_pass", "ntt_inv_last_pass"):
+    if name.startswith("ntt_fwd_") or name.startswith("ntt_inv_"):
         return 48.0 * L
     if name == "ntt_pointwise":
         return 72.0 * L
@@ -62,6 +62,23 @@ def mul_algorithmic_bytes(na: int, nb: int, L: int) -> float:
     with the pointwise product and the inverse row pass), the inverse column
     pass fused with CRT and carry."""
     return 16.0 * (na + nb) + 192.0 * L
+
+
+def measured_traffic(kernel: str, L: int):
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum)
+    from the committed ncu summary profiles/traffic.txt, whose lines read
+    `<kernel> <bytes per launch> <transform length L of the capture>`; the
+    capture is taken on a smaller case and scaled by L, since a pass moves
+    every residue once."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    try:
+        for line in open(path):
+            f = line.split()
+            if len(f) >= 3 and f[0] == kernel and not line.startswith("#"):
+                return float(f[1]) * L / float(f[2])
+    except OSError:
+        pass
+    return None
 
 
 def peaks() -> tuple[float, str]:
@@ -278,13 +295,7 @@ def main() -> None:
     d_avg = dms / dcount
     d_bytes = kernel_bytes(dname, n, n, L)
     achieved = d_bytes / (d_avg / 1e3) / 1e9
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath):
-        try:
-            traffic = json.load(open(tpath)).get(dname)
-        except Exception:
-            traffic = None
+    traffic = measured_traffic(dname, L)
     mul_bytes = mul_algorithmic_bytes(n, n, L)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,

@@ -42,8 +42,10 @@ typedef struct nn_transform nn_transform;
 /* Creates a context on `device`.  hbm_budget_bytes = 0 means no budget. */
 nn_status nn_context_create(int device, uint64_t hbm_budget_bytes, nn_context** out);
 nn_status nn_context_destroy(nn_context* ctx);
-/* Use a caller-owned cudaStream_t (NULL restores the context's own stream). */
+/* Order all work on a caller-owned cudaStream_t (NULL = the legacy default stream). */
 nn_status nn_context_set_stream(nn_context* ctx, void* cuda_stream);
+/* Go back to the context's own non-blocking stream (the initial state). */
+nn_status nn_context_use_own_stream(nn_context* ctx);
 void* nn_context_stream(nn_context* ctx);
 /* Waits for the stream and reports any deferred device-side error. */
 nn_status nn_context_synchronize(nn_context* ctx);

@@ -55,6 +55,7 @@ def lib() -> C.CDLL:
         "nn_context_create": (C.c_int, [C.c_int, C.c_uint64, C.POINTER(_vp)]),
         "nn_context_destroy": (C.c_int, [_vp]),
         "nn_context_set_stream": (C.c_int, [_vp, _vp]),
+        "nn_context_use_own_stream": (C.c_int, [_vp]),
         "nn_context_stream": (_vp, [_vp]),
         "nn_context_synchronize": (C.c_int, [_vp]),
         "nn_status_string": (C.c_char_p, [C.c_int]),
@@ -138,7 +139,12 @@ class Context:
             pass
 
     def set_stream(self, stream_ptr: int | None) -> None:
-        self._check(lib().nn_context_set_stream(self.h, _vp(stream_ptr or 0)), "set_stream")
+        """Order work on a cudaStream_t handle (0 = the legacy default stream);
+        None returns to the context's own stream."""
+        if stream_ptr is None:
+            self._check(lib().nn_context_use_own_stream(self.h), "use_own_stream")
+        else:
+            self._check(lib().nn_context_set_stream(self.h, _vp(stream_ptr)), "set_stream")
 
     def synchronize(self) -> None:
         self._check(lib().nn_context_synchronize(self.h), "synchronize")

@@ -292,7 +292,13 @@ nn_status nn_context_destroy(nn_context* c) {
 
 nn_status nn_context_set_stream(nn_context* c, void* s) {
   if (!c) return NN_ERR_INVALID;
-  c->stream = s ? (cudaStream_t)s : c->own;
+  c->stream = (cudaStream_t)s;  // NULL is the legacy default stream, as in CUDA
+  return NN_OK;
+}
+
+nn_status nn_context_use_own_stream(nn_context* c) {
+  if (!c) return NN_ERR_INVALID;
+  c->stream = c->own;
   return NN_OK;
 }
 

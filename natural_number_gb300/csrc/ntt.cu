@@ -249,7 +249,12 @@ cudaError_t launch_pass(const u64* in, u64* out, u64 n_in, int s, const Pass& ps
   }
   const u64 tiles = (1ull << s) / ((u64)ps.C << ps.R);
   dim3 grid((unsigned)tiles, 3);
-  launch_begin(FIRST ? "ntt_fwd_load_pass" : INV ? (SCALE ? "ntt_inv_last_pass" : "ntt_inv_pass") : "ntt_fwd_pass", st);
+  const char* name = C == 2 ? (INV ? "ntt_inv_row_pass" : "ntt_fwd_row_pass")
+                            : FIRST ? "ntt_fwd_load_col_pass"
+                                    : INV ? (SCALE ? "ntt_inv_last_col_pass" : "ntt_inv_col_pass") : "ntt_fwd_col_pass";
+  if (C == 2 && FIRST) name = "ntt_fwd_load_row_pass";
+  if (C == 2 && SCALE) name = "ntt_inv_last_row_pass";
+  launch_begin(name, st);
   ntt_pass_kernel<C, FIRST, INV, SCALE><<<grid, 256, smem, st>>>(in, out, n_in, s, ps.lambda0, ps.R,
                                                                   INV ? t.iroot : t.root, t.cap);
   launch_end(st);
