@@ -101,10 +101,42 @@ void nn_profile_enable(int on);
 uint64_t nn_profile_report(char* buf, uint64_t cap);
 
 /* ---- host-pointer entry points (copy in, compute, copy out) ------------- */
+/* Process-wide context on the current device, created on first use. */
+nn_context* nn_default_context(void);
+/* nn_transform_forward from host limbs (staged through device scratch). */
+nn_status nn_transform_forward_host(nn_context* ctx, nn_transform* t, const uint64_t* limbs, uint64_t n, int scale);
+/* nn_transform_inverse_save into host memory (out: max(size, 2^scale) limbs). */
+nn_status nn_transform_inverse_save_host(nn_context* ctx, nn_transform* t, uint64_t* out, uint64_t size,
+                                         uint64_t* written);
+/* Schoolbook product on the GPU from host limbs: out holds n_a + n_b limbs (not normalised). */
+nn_status nn_mul_base_host(nn_context* ctx, uint64_t* out, const uint64_t* a, uint64_t n_a, const uint64_t* b,
+                           uint64_t n_b);
 /* *out_n receives the normalised limb count; out holds n_a + n_b limbs. */
 nn_status nn_mul_host(nn_context* ctx, uint64_t* out, uint64_t* out_n, const uint64_t* a, uint64_t n_a,
                       const uint64_t* b, uint64_t n_b);
 nn_status nn_sqr_host(nn_context* ctx, uint64_t* out, uint64_t* out_n, const uint64_t* a, uint64_t n);
+
+/* ---- natural-level algorithms on host limbs (products on the GPU) -------- */
+/* Results are malloc'd little-endian limbs (release with nn_free); sizes are
+ * as the reference's natural holds them (natural::std normalisation where it
+ * applies). */
+void nn_free(void* p);
+/* natural::_div (natural.h:749-769): quotient and remainder. */
+nn_status nn_div_host(nn_context* ctx, const uint64_t* a, uint64_t n_a, const uint64_t* b, uint64_t n_b,
+                      uint64_t** q, uint64_t* q_n, uint64_t** r, uint64_t* r_n);
+/* pow (natural.h:554-564). */
+nn_status nn_pow_host(nn_context* ctx, const uint64_t* b, uint64_t n_b, uint64_t e, uint64_t** out, uint64_t* out_n);
+/* reciprocal(divs, divd_size) (natural.h:575-617) and the division variant
+ * reciprocal(divisor, dividend_size, NTT_info&) (natural.h:619-687); the
+ * divisor's top limb must be 1. */
+nn_status nn_reciprocal_host(nn_context* ctx, const uint64_t* d, uint64_t n_d, uint64_t divd_size, int variant,
+                             uint64_t** out, uint64_t* out_n);
+/* Decimal digits of a natural (std::formatter<natural>, natural.h:1089-1091). */
+nn_status nn_to_dec_host(nn_context* ctx, const uint64_t* a, uint64_t n_a, char** out, uint64_t* len);
+/* The reference's pi and e recipes (calc_pi + sqrt_10005, calc_e; natural.h:841-902,
+ * test.cpp:12-32): decimal digit strings. */
+nn_status nn_pi_dec_host(nn_context* ctx, uint64_t terms, uint64_t acc, uint64_t digits, char** out, uint64_t* len);
+nn_status nn_e_dec_host(nn_context* ctx, uint64_t terms, uint64_t digits, char** out, uint64_t* len);
 
 #ifdef __cplusplus
 }

@@ -76,6 +76,18 @@ def lib() -> C.CDLL:
         "nn_launch_count": (C.c_uint64, []),
         "nn_profile_enable": (None, [C.c_int]),
         "nn_profile_report": (C.c_uint64, [C.c_char_p, C.c_uint64]),
+        "nn_free": (None, [_vp]),
+        "nn_div_host": (C.c_int, [_vp, _u64p, C.c_uint64, _u64p, C.c_uint64, C.POINTER(_u64p), _u64p,
+                                  C.POINTER(_u64p), _u64p]),
+        "nn_pow_host": (C.c_int, [_vp, _u64p, C.c_uint64, C.c_uint64, C.POINTER(_u64p), _u64p]),
+        "nn_reciprocal_host": (C.c_int, [_vp, _u64p, C.c_uint64, C.c_uint64, C.c_int, C.POINTER(_u64p), _u64p]),
+        "nn_to_dec_host": (C.c_int, [_vp, _u64p, C.c_uint64, C.POINTER(_vp), _u64p]),
+        "nn_pi_dec_host": (C.c_int, [_vp, C.c_uint64, C.c_uint64, C.c_uint64, C.POINTER(_vp), _u64p]),
+        "nn_e_dec_host": (C.c_int, [_vp, C.c_uint64, C.c_uint64, C.POINTER(_vp), _u64p]),
+        "nn_mul_base_host": (C.c_int, [_vp, _u64p, _u64p, C.c_uint64, _u64p, C.c_uint64]),
+        "nn_default_context": (_vp, []),
+        "nn_transform_forward_host": (C.c_int, [_vp, _vp, _u64p, C.c_uint64, C.c_int]),
+        "nn_transform_inverse_save_host": (C.c_int, [_vp, _vp, _u64p, C.c_uint64, _u64p]),
         "nn_mul_host": (C.c_int, [_vp, _u64p, _u64p, _u64p, C.c_uint64, _u64p, C.c_uint64]),
         "nn_sqr_host": (C.c_int, [_vp, _u64p, _u64p, _u64p, C.c_uint64]),
     }
@@ -173,6 +185,60 @@ class Context:
         n = C.c_uint64()
         self._check(lib().nn_sqr_host(self.h, _ptr(out), C.byref(n), _ptr(a), a.size), "sqr")
         return out[: n.value]
+
+    def _take(self, p, n) -> np.ndarray:
+        out = np.ctypeslib.as_array(p, shape=(max(n, 1),))[:n].copy()
+        lib().nn_free(C.cast(p, _vp))
+        return out
+
+    def _take_str(self, p, n) -> str:
+        s = C.string_at(p, n).decode()
+        lib().nn_free(p)
+        return s
+
+    def mul_base(self, a, b) -> np.ndarray:
+        """Schoolbook product on the GPU (n_a + n_b limbs, not normalised)."""
+        a, b = _np(a), _np(b)
+        out = np.empty(a.size + b.size, dtype=np.uint64)
+        self._check(lib().nn_mul_base_host(self.h, _ptr(out), _ptr(a), a.size, _ptr(b), b.size), "mul_base")
+        return out
+
+    def div(self, a, b) -> tuple[np.ndarray, np.ndarray]:
+        """natural::_div: (quotient, remainder) with the reference's sizes."""
+        a, b = _np(a), _np(b)
+        q, r, qn, rn = _u64p(), _u64p(), C.c_uint64(), C.c_uint64()
+        self._check(lib().nn_div_host(self.h, _ptr(a), a.size, _ptr(b), b.size, C.byref(q), C.byref(qn),
+                                      C.byref(r), C.byref(rn)), "div")
+        return self._take(q, qn.value), self._take(r, rn.value)
+
+    def pow(self, b, e: int) -> np.ndarray:
+        b = _np(b)
+        p, n = _u64p(), C.c_uint64()
+        self._check(lib().nn_pow_host(self.h, _ptr(b), b.size, e, C.byref(p), C.byref(n)), "pow")
+        return self._take(p, n.value)
+
+    def reciprocal(self, d, divd_size: int, variant: int = 2) -> np.ndarray:
+        d = _np(d)
+        p, n = _u64p(), C.c_uint64()
+        self._check(lib().nn_reciprocal_host(self.h, _ptr(d), d.size, divd_size, variant, C.byref(p), C.byref(n)),
+                    "reciprocal")
+        return self._take(p, n.value)
+
+    def to_dec(self, a) -> str:
+        a = _np(a)
+        p, n = _vp(), C.c_uint64()
+        self._check(lib().nn_to_dec_host(self.h, _ptr(a), a.size, C.byref(p), C.byref(n)), "to_dec")
+        return self._take_str(p, n.value)
+
+    def pi_dec(self, terms: int, acc: int, digits: int) -> str:
+        p, n = _vp(), C.c_uint64()
+        self._check(lib().nn_pi_dec_host(self.h, terms, acc, digits, C.byref(p), C.byref(n)), "pi_dec")
+        return self._take_str(p, n.value)
+
+    def e_dec(self, terms: int, digits: int) -> str:
+        p, n = _vp(), C.c_uint64()
+        self._check(lib().nn_e_dec_host(self.h, terms, digits, C.byref(p), C.byref(n)), "e_dec")
+        return self._take_str(p, n.value)
 
     # -- device-pointer API ---------------------------------------------------
     def mul_device(self, out, a, b, na: int | None = None, nb: int | None = None) -> None:

@@ -32,6 +32,8 @@ struct nn_context {
   nn::Tables tables;
   nn::Scan scan;
   std::string err;
+  u64* scratch[3] = {nullptr, nullptr, nullptr};  // grow-only device staging for host calls
+  u64 scratch_words[3] = {0, 0, 0};
 };
 
 struct nn_transform {
@@ -208,6 +210,21 @@ nn_status sqr_impl(nn_context* c, u64* d_out, const u64* a, u64 n) {
   return st;
 }
 
+// Grow-only device staging buffer `slot` of at least `words` limbs.
+nn_status scratch(nn_context* c, int slot, u64 words, u64** p) {
+  if (c->scratch_words[slot] < words) {
+    dev_free(c, c->scratch[slot], c->scratch_words[slot]);
+    c->scratch[slot] = nullptr;
+    c->scratch_words[slot] = 0;
+    u64 w = std::bit_ceil(std::max<u64>(words, 1024));
+    nn_status st = dev_alloc(c, &c->scratch[slot], w);
+    if (st != NN_OK) return st;
+    c->scratch_words[slot] = w;
+  }
+  *p = c->scratch[slot];
+  return NN_OK;
+}
+
 u64 normalized(const u64* x, u64 n) {  // natural::std (natural.h:82-93)
   while (n > 1 && x[n - 1] == 0) --n;
   return n;
@@ -282,6 +299,8 @@ nn_status nn_context_create(int device, uint64_t budget, nn_context** out) {
 nn_status nn_context_destroy(nn_context* c) {
   if (!c) return NN_ERR_INVALID;
   cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (int i = 0; i < 3; ++i) dev_free(c, c->scratch[i], c->scratch_words[i]);
   cudaStreamSynchronize(c->stream);
   nn::tables_free(c->tables);
   nn::scan_free(c->scan);
@@ -391,16 +410,16 @@ nn_status nn_mul_base(nn_context* c, uint64_t* d_out, const uint64_t* a, uint64_
 nn_status nn_mul_host(nn_context* c, uint64_t* out, uint64_t* out_n, const uint64_t* a, uint64_t na,
                       const uint64_t* b, uint64_t nb) {
   if (!c || !out || !a || !b || !na || !nb) return NN_ERR_INVALID;
-  DBuf da(c), db(c), dout(c);
-  nn_status st = da.alloc(na);
-  if (st == NN_OK) st = db.alloc(nb);
-  if (st == NN_OK) st = dout.alloc(na + nb);
+  u64 *da, *db, *dout;
+  nn_status st = scratch(c, 0, na, &da);
+  if (st == NN_OK) st = scratch(c, 1, nb, &db);
+  if (st == NN_OK) st = scratch(c, 2, na + nb, &dout);
   if (st != NN_OK) return st;
-  NN_CK(c, cudaMemcpyAsync(da.p, a, na * 8, cudaMemcpyHostToDevice, c->stream), "H2D");
-  NN_CK(c, cudaMemcpyAsync(db.p, b, nb * 8, cudaMemcpyHostToDevice, c->stream), "H2D");
-  st = mul_impl(c, dout.p, da.p, na, db.p, nb);
+  NN_CK(c, cudaMemcpyAsync(da, a, na * 8, cudaMemcpyHostToDevice, c->stream), "H2D");
+  NN_CK(c, cudaMemcpyAsync(db, b, nb * 8, cudaMemcpyHostToDevice, c->stream), "H2D");
+  st = mul_impl(c, dout, da, na, db, nb);
   if (st != NN_OK) return st;
-  NN_CK(c, cudaMemcpyAsync(out, dout.p, (na + nb) * 8, cudaMemcpyDeviceToHost, c->stream), "D2H");
+  NN_CK(c, cudaMemcpyAsync(out, dout, (na + nb) * 8, cudaMemcpyDeviceToHost, c->stream), "D2H");
   st = nn_context_synchronize(c);
   if (st == NN_OK && out_n) *out_n = normalized(out, na + nb);
   return st;
@@ -408,17 +427,69 @@ nn_status nn_mul_host(nn_context* c, uint64_t* out, uint64_t* out_n, const uint6
 
 nn_status nn_sqr_host(nn_context* c, uint64_t* out, uint64_t* out_n, const uint64_t* a, uint64_t n) {
   if (!c || !out || !a || !n) return NN_ERR_INVALID;
-  DBuf da(c), dout(c);
-  nn_status st = da.alloc(n);
-  if (st == NN_OK) st = dout.alloc(2 * n);
+  u64 *da, *dout;
+  nn_status st = scratch(c, 0, n, &da);
+  if (st == NN_OK) st = scratch(c, 2, 2 * n, &dout);
   if (st != NN_OK) return st;
-  NN_CK(c, cudaMemcpyAsync(da.p, a, n * 8, cudaMemcpyHostToDevice, c->stream), "H2D");
-  st = sqr_impl(c, dout.p, da.p, n);
+  NN_CK(c, cudaMemcpyAsync(da, a, n * 8, cudaMemcpyHostToDevice, c->stream), "H2D");
+  st = sqr_impl(c, dout, da, n);
   if (st != NN_OK) return st;
-  NN_CK(c, cudaMemcpyAsync(out, dout.p, 2 * n * 8, cudaMemcpyDeviceToHost, c->stream), "D2H");
+  NN_CK(c, cudaMemcpyAsync(out, dout, 2 * n * 8, cudaMemcpyDeviceToHost, c->stream), "D2H");
   st = nn_context_synchronize(c);
   if (st == NN_OK && out_n) *out_n = normalized(out, 2 * n);
   return st;
+}
+
+nn_status nn_mul_base_host(nn_context* c, uint64_t* out, const uint64_t* a, uint64_t na, const uint64_t* b,
+                           uint64_t nb) {
+  if (!c || !out || !a || !b || !na || !nb) return NN_ERR_INVALID;
+  u64 *da, *db, *dout;
+  nn_status st = scratch(c, 0, na, &da);
+  if (st == NN_OK) st = scratch(c, 1, nb, &db);
+  if (st == NN_OK) st = scratch(c, 2, na + nb, &dout);
+  if (st != NN_OK) return st;
+  NN_CK(c, cudaMemcpyAsync(da, a, na * 8, cudaMemcpyHostToDevice, c->stream), "H2D");
+  NN_CK(c, cudaMemcpyAsync(db, b, nb * 8, cudaMemcpyHostToDevice, c->stream), "H2D");
+  NN_CK(c, nn::school_mul(da, na, db, nb, dout, c->scan, c->stream), "base-case product");
+  NN_CK(c, cudaMemcpyAsync(out, dout, (na + nb) * 8, cudaMemcpyDeviceToHost, c->stream), "D2H");
+  return nn_context_synchronize(c);
+}
+
+nn_status nn_transform_forward_host(nn_context* c, nn_transform* t, const uint64_t* limbs, uint64_t n, int s) {
+  if (!c || !t || !limbs || !n) return NN_ERR_INVALID;
+  u64* d;
+  nn_status st = scratch(c, 0, n, &d);
+  if (st != NN_OK) return st;
+  NN_CK(c, cudaMemcpyAsync(d, limbs, n * 8, cudaMemcpyHostToDevice, c->stream), "H2D");
+  return forward(c, t, d, n, s);
+}
+
+nn_status nn_transform_inverse_save_host(nn_context* c, nn_transform* t, uint64_t* out, uint64_t size,
+                                         uint64_t* written) {
+  if (!c || !t || !t->res || !out) return NN_ERR_INVALID;
+  const u64 L = 1ull << t->scale;
+  u64* d;
+  nn_status st = scratch(c, 2, std::max<u64>(size, L), &d);
+  if (st != NN_OK) return st;
+  u64 w = 0;
+  st = inverse_save(c, t, d, size, &w);
+  if (st != NN_OK) return st;
+  NN_CK(c, cudaMemcpyAsync(out, d, w * 8, cudaMemcpyDeviceToHost, c->stream), "D2H");
+  st = nn_context_synchronize(c);
+  if (written) *written = w;
+  return st;
+}
+
+nn_context* nn_default_context(void) {
+  static nn_context* ctx = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (nn_context_create(dev, 0, &ctx) != NN_OK) ctx = nullptr;
+  }
+  return ctx;
 }
 
 }  // extern "C"

@@ -32,6 +32,7 @@ static __constant__ PrimeSet g_primes;
   cudaError_t name(const PrimeSet& ps) { return cudaMemcpyToSymbol(g_primes, &ps, sizeof ps); }
 cudaError_t upload_primes_ntt(const PrimeSet& ps);
 cudaError_t upload_primes_carry(const PrimeSet& ps);
+cudaError_t upload_primes_batch(const PrimeSet& ps);
 
 __device__ __forceinline__ u64 mulhi(u64 a, u64 b) { return __umul64hi(a, b); }
 

@@ -34,7 +34,9 @@ void tables_free(Tables& t);
 struct Pass {
   int lambda0, R, C;
 };
-std::vector<Pass> plan_passes(int s);
+// r_last: levels of the contiguous (deepest) pass; r_col: most levels of a
+// strided column pass.
+std::vector<Pass> plan_passes(int s, int r_last = 11, int r_col = 9);
 
 // Scratch for the decoupled-lookback carry scan.
 struct Scan {
@@ -48,13 +50,41 @@ constexpr int kScanThreads = 256;
 constexpr int kScanE = 8;  // limbs per thread
 constexpr u64 kScanTile = (u64)kScanThreads * kScanE;
 
+// Batched products (batch.cu): jobs, their work items, and the launch.
+enum : unsigned char { kItemFwd = 0, kItemPointwise = 1, kItemInv = 2, kItemCrt = 3, kItemColumn = 4 };
+struct BatchJob {
+  const u64* a;
+  const u64* b;
+  u64* out;      // na + nb limbs
+  u64 na, nb;
+  u64* res_a;    // [3][2^s] residues (NTT jobs)
+  u64* res_b;
+  u32 ctr_base;  // first (job, step) completion counter
+  u32 flag_base; // first carry-scan status word
+  int s;         // transform scale; 0 for a schoolbook job
+  int square;    // a == b: one transform
+  int n_pass;
+  int lambda0[4], R[4], C[4];
+};
+struct BatchItem {
+  u32 job;
+  unsigned short step;
+  unsigned char kind, pass, prime, operand;
+  unsigned short pad;
+  u32 tile;
+};
+cudaError_t batch_configure(int* blocks_per_sm, size_t smem);
+cudaError_t batch_launch(const BatchJob* jobs, const BatchItem* items, u32 n_items, const u32* need, u32* done,
+                         u32* head, u32* flags, u32* err, const Tables& t, int grid, size_t smem, cudaStream_t st);
+
 // Forward transform: limbs (n <= 2^s) -> residues [3][2^s], raw values in
 // [0,2p) identical to NTT_info::load + NTT (ntt_info.h:147-198).
-cudaError_t ntt_forward(const u64* limbs, u64 n, u64* res, int s, const Tables& t, cudaStream_t st);
+cudaError_t ntt_forward(const u64* limbs, u64 n, u64* res, int s, const Tables& t, cudaStream_t st,
+                        const std::vector<Pass>* plan = nullptr);
 // Pointwise product of degree-1 residues (ntt_info.h:224-231); dst may alias a or b.
 cudaError_t ntt_pointwise(u64* dst, const u64* a, const u64* b, int s, const Tables& t, cudaStream_t st);
 // Inverse transform with the final 2^-(s-1) scale (ntt_info.h:200-221); values in [0,p).
-cudaError_t ntt_inverse(u64* res, int s, const Tables& t, cudaStream_t st);
+cudaError_t ntt_inverse(u64* res, int s, const Tables& t, cudaStream_t st, const std::vector<Pass>* plan = nullptr);
 // CRT + carry into `size` limbs (normal mode) or the wrapped product mod
 // B^L - 1 in L limbs when size-1 > L (ntt_info.h:237-248).  Returns the
 // number of limbs written through *written (host value).

@@ -23,6 +23,7 @@
 
 #include "nn_device.cuh"
 #include "nn_internal.h"
+#include "ntt_tiles.cuh"
 
 namespace nn {
 
@@ -91,150 +92,20 @@ __global__ void twiddle_extend_kernel(u64* tab, u64 n, u64 bw, u64 bwp, int prim
 // Tiled passes
 // ---------------------------------------------------------------------------
 
-template <int K, int C, bool INV>
-__device__ __forceinline__ void level_group(u64* sm, int l, int R, u64 ksb, const u64* __restrict__ tw, u64 p,
-                                            u32 ch) {
-  const int nsub = R - l - K;
-  const int units = C << (R - K);
-  for (int u = threadIdx.x; u < units; u += blockDim.x) {
-    const int i = u & (C - 1);
-    const int v = u / C;
-    const int t0 = v & ((1 << nsub) - 1);
-    const int rb = v >> nsub;
-    const int row0 = (rb << (R - l)) + t0;
-    const int rstep = 1 << nsub;
-    const u64 bidx = (ksb << l) + (u64)rb;
-    u64 x[1 << K];
-#pragma unroll
-    for (int m = 0; m < (1 << K); ++m) x[m] = sm[(row0 + m * rstep) * C + i];
-    if (!INV) {
-#pragma unroll
-      for (int lv = 0; lv < K; ++lv) {
-        const int half = (1 << K) >> (lv + 1);
-#pragma unroll
-        for (int g = 0; g < (1 << lv); ++g) {
-          const ulonglong2 wv = __ldg(reinterpret_cast<const ulonglong2*>(tw) + ((bidx << lv) + g));
-#pragma unroll
-          for (int m = 0; m < half; ++m) fwd_bfly(x[g * 2 * half + m], x[g * 2 * half + m + half], wv.x, wv.y, p, ch);
-        }
-      }
-    } else {
-#pragma unroll
-      for (int lv = K - 1; lv >= 0; --lv) {
-        const int half = (1 << K) >> (lv + 1);
-#pragma unroll
-        for (int g = 0; g < (1 << lv); ++g) {
-          const ulonglong2 wv = __ldg(reinterpret_cast<const ulonglong2*>(tw) + ((bidx << lv) + g));
-#pragma unroll
-          for (int m = 0; m < half; ++m) inv_bfly(x[g * 2 * half + m], x[g * 2 * half + m + half], wv.x, wv.y, p, ch);
-        }
-      }
-    }
-#pragma unroll
-    for (int m = 0; m < (1 << K); ++m) sm[(row0 + m * rstep) * C + i] = x[m];
-  }
-}
-
 // FIRST: input is limbs (n_in of them, zero beyond); otherwise residues [3][L].
 // SCALE: multiply by 2^-(s-1) on the way out (last inverse pass).
 template <int C, bool FIRST, bool INV, bool SCALE>
 __global__ void __launch_bounds__(256) ntt_pass_kernel(const u64* in, u64* out, u64 n_in, int s, int lambda0, int R,
                                                        const u64* __restrict__ tab, u64 tab_stride) {
   extern __shared__ u64 sm[];
-  const int prime = blockIdx.y;
-  const u64 p = g_primes.p[prime];
-  const u32 ch = g_primes.c_hi[prime];
-  const u64 L = 1ull << s;
-  const u64* tw = tab + (u64)prime * tab_stride;
-  const int lg_s = s - lambda0 - R;
-  const u64 tiles_per_sb = (1ull << lg_s) / C;
-  const u64 tile = blockIdx.x;
-  const u64 ksb = tile / tiles_per_sb;
-  const u64 base = (ksb << (lg_s + R)) + (tile % tiles_per_sb) * C;
-  const int nel = C << R;
-
-  if (FIRST) {
-    const u64 m64 = g_primes.m64[prime];
-    for (int idx = threadIdx.x; idx < nel; idx += blockDim.x) {
-      const u64 pos = base + ((u64)(idx / C) << lg_s) + (idx & (C - 1));
-      sm[idx] = pos < n_in ? limb_mod(in[pos], m64, p, ch) : 0;
-    }
-  } else {
-    const u64* src = in + (u64)prime * L;
-    for (int idx = 2 * threadIdx.x; idx < nel; idx += 2 * blockDim.x) {
-      const u64 pos = base + ((u64)(idx / C) << lg_s) + (idx & (C - 1));
-      const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(src + pos);
-      sm[idx] = v.x;
-      sm[idx + 1] = v.y;
-    }
-  }
-  __syncthreads();
-
-  if (!INV) {
-    for (int l = 0; l < R;) {
-      const int k = R - l >= 3 ? 3 : R - l;
-      if (k == 3)
-        level_group<3, C, false>(sm, l, R, ksb, tw, p, ch);
-      else if (k == 2)
-        level_group<2, C, false>(sm, l, R, ksb, tw, p, ch);
-      else
-        level_group<1, C, false>(sm, l, R, ksb, tw, p, ch);
-      __syncthreads();
-      l += k;
-    }
-  } else {
-    for (int l = R; l > 0;) {
-      const int k = l >= 3 ? 3 : l;
-      l -= k;
-      if (k == 3)
-        level_group<3, C, true>(sm, l, R, ksb, tw, p, ch);
-      else if (k == 2)
-        level_group<2, C, true>(sm, l, R, ksb, tw, p, ch);
-      else
-        level_group<1, C, true>(sm, l, R, ksb, tw, p, ch);
-      __syncthreads();
-    }
-  }
-
-  u64* dst = out + (u64)prime * L;
-  for (int idx = 2 * threadIdx.x; idx < nel; idx += 2 * blockDim.x) {
-    const u64 pos = base + ((u64)(idx / C) << lg_s) + (idx & (C - 1));
-    ulonglong2 v = make_ulonglong2(sm[idx], sm[idx + 1]);
-    if (SCALE) {
-      v.x = div_pow2(v.x, (u32)(s - 1), p);
-      v.y = div_pow2(v.y, (u32)(s - 1), p);
-    }
-    *reinterpret_cast<ulonglong2*>(dst + pos) = v;
-  }
+  pass_tile<C, FIRST, INV, SCALE, false>(sm, in, out, n_in, s, lambda0, R, tab, tab_stride, blockIdx.y, blockIdx.x);
 }
 
-// Pointwise product of the degree-1 residues (a0 + a1 x)(b0 + b1 x) mod
-// (x^2 - w) and (a2 + a3 x)(b2 + b3 x) mod (x^2 + w), w = root[2g]
-// (ntt_info.h:224-231, asmLinux.asm:910-1057).  Inputs in [0,2p), outputs in [0,p).
 __global__ void __launch_bounds__(256) pointwise_kernel(u64* dst, const u64* a, const u64* b, u64 L,
                                                         const u64* __restrict__ tab, u64 tab_stride) {
-  const int i = blockIdx.y;
   const u64 g = (u64)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= L / 4) return;
-  const u64 p = g_primes.p[i];
-  const u32 ch = g_primes.c_hi[i];
-  const ulonglong2 wv = __ldg(reinterpret_cast<const ulonglong2*>(tab + (u64)i * tab_stride) + g);
-  const ulonglong2* A = reinterpret_cast<const ulonglong2*>(a + (u64)i * L) + 2 * g;
-  const ulonglong2* B = reinterpret_cast<const ulonglong2*>(b + (u64)i * L) + 2 * g;
-  ulonglong2 A0 = A[0], A1 = A[1], B0 = B[0], B1 = B[1];
-  const u64 a0 = reduce2p(A0.x, p), a1 = reduce2p(A0.y, p), a2 = reduce2p(A1.x, p), a3 = reduce2p(A1.y, p);
-  const u64 b0 = reduce2p(B0.x, p), b1 = reduce2p(B0.y, p), b2 = reduce2p(B1.x, p), b3 = reduce2p(B1.y, p);
-  const u64 wb1 = shoup_mul(b1, wv.x, wv.y, p, ch);
-  const u64 wb3 = shoup_mul(b3, wv.x, wv.y, p, ch);
-  const u64 nwb3 = wb3 ? p - wb3 : 0;
-  ulonglong2 R0, R1;
-  R0.x = barrett(add128(mul_wide(a0, b0), mul_wide(a1, wb1)), i);
-  R0.y = barrett(add128(mul_wide(a0, b1), mul_wide(a1, b0)), i);
-  R1.x = barrett(add128(mul_wide(a2, b2), mul_wide(a3, nwb3)), i);
-  R1.y = barrett(add128(mul_wide(a2, b3), mul_wide(a3, b2)), i);
-  ulonglong2* D = reinterpret_cast<ulonglong2*>(dst + (u64)i * L) + 2 * g;
-  D[0] = R0;
-  D[1] = R1;
+  pointwise_group<false>(dst, a, b, L, tab, tab_stride, blockIdx.y, g);
 }
 
 template <int C, bool FIRST, bool INV, bool SCALE>
@@ -276,7 +147,8 @@ void primes_host(u64 p[3]) {
 cudaError_t upload_primes() {
   PrimeSet ps = make_primes();
   cudaError_t e = upload_primes_ntt(ps);
-  return e == cudaSuccess ? upload_primes_carry(ps) : e;
+  if (e == cudaSuccess) e = upload_primes_carry(ps);
+  return e == cudaSuccess ? upload_primes_batch(ps) : e;
 }
 
 cudaError_t tables_ensure(Tables& t, int s, cudaStream_t st) {
@@ -337,15 +209,17 @@ void tables_free(Tables& t) {
   t = Tables{};
 }
 
-std::vector<Pass> plan_passes(int s) {
+std::vector<Pass> plan_passes(int s, int r_last_max, int r_col) {
   // Levels 0..s-2.  The deepest pass works on contiguous blocks (C = 2 columns
-  // of stride 2) of up to 2^12 words; the levels above it go in strided
-  // passes of at most 9 levels with 16-column (128-byte) row segments.
+  // of stride 2) of up to 2^(r_last_max+1) words; the levels above it go in
+  // strided passes of at most r_col levels with 16-column (128-byte) rows.
   std::vector<Pass> out;
   const int total = s - 1;
-  const int r_last = std::min(total, 11);
+  r_last_max = std::max(3, std::min(r_last_max, 12));
+  r_col = std::max(1, std::min(r_col, 9));
+  const int r_last = std::min(total, r_last_max);
   int rest = total - r_last;
-  const int n_mid = (rest + 8) / 9;
+  const int n_mid = (rest + r_col - 1) / r_col;
   int l = 0;
   for (int k = 0; k < n_mid; ++k) {
     int r = rest / (n_mid - k);
@@ -357,8 +231,9 @@ std::vector<Pass> plan_passes(int s) {
   return out;
 }
 
-cudaError_t ntt_forward(const u64* limbs, u64 n, u64* res, int s, const Tables& t, cudaStream_t st) {
-  std::vector<Pass> plan = plan_passes(s);
+cudaError_t ntt_forward(const u64* limbs, u64 n, u64* res, int s, const Tables& t, cudaStream_t st,
+                        const std::vector<Pass>* given) {
+  std::vector<Pass> plan = given ? *given : plan_passes(s);
   for (size_t k = 0; k < plan.size(); ++k) {
     cudaError_t e = k == 0 ? dispatch_pass<true, false, false>(limbs, res, n, s, plan[k], t, st)
                            : dispatch_pass<false, false, false>(res, res, 0, s, plan[k], t, st);
@@ -367,8 +242,8 @@ cudaError_t ntt_forward(const u64* limbs, u64 n, u64* res, int s, const Tables& 
   return cudaSuccess;
 }
 
-cudaError_t ntt_inverse(u64* res, int s, const Tables& t, cudaStream_t st) {
-  std::vector<Pass> plan = plan_passes(s);
+cudaError_t ntt_inverse(u64* res, int s, const Tables& t, cudaStream_t st, const std::vector<Pass>* given) {
+  std::vector<Pass> plan = given ? *given : plan_passes(s);
   for (size_t k = plan.size(); k-- > 0;) {
     cudaError_t e = k == 0 ? dispatch_pass<false, true, true>(res, res, 0, s, plan[k], t, st)
                            : dispatch_pass<false, true, false>(res, res, 0, s, plan[k], t, st);
