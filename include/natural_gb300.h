@@ -91,6 +91,38 @@ nn_status nn_ntt_mul(nn_context* ctx, uint64_t* d_out, const uint64_t* d_a, uint
 nn_status nn_mul_base(nn_context* ctx, uint64_t* d_out, const uint64_t* d_a, uint64_t n_a, const uint64_t* d_b,
                       uint64_t n_b);
 
+/* ---- batches: many products in one persistent launch -------------------- */
+/* One product of a batch (device pointers; d_out holds n_a + n_b limbs, not
+ * normalised).  d_a == d_b with n_a == n_b is a square (one transform). */
+typedef struct {
+  const uint64_t* d_a;
+  uint64_t n_a;
+  const uint64_t* d_b;
+  uint64_t n_b;
+  uint64_t* d_out;
+} nn_mul_job;
+typedef struct nn_batch nn_batch;
+/* Plans a batch for these operand sizes (the reference has no batch API;
+ * each job is natural::_mul, natural.h:444-450): jobs whose shorter operand
+ * is below the "batch_ntt_min" tunable run as schoolbook column scans, the
+ * others as three-prime NTT products at scale ceil(log2(n_a+n_b-1)).  All
+ * pipelines go into one work queue drained by one persistent launch; the
+ * launch sequence is captured in a CUDA graph on first run and replayed.
+ * square[j] (optional) marks squares. */
+nn_status nn_batch_create(nn_context* ctx, const uint64_t* n_a, const uint64_t* n_b, const int* square,
+                          uint64_t count, nn_batch** out);
+/* Runs the planned batch on these operands (sizes must match the plan). */
+nn_status nn_batch_run(nn_context* ctx, nn_batch* batch, const nn_mul_job* jobs);
+nn_status nn_batch_destroy(nn_context* ctx, nn_batch* batch);
+uint64_t nn_batch_items(const nn_batch* batch);
+/* Plan + run + release in one call. */
+nn_status nn_batch_mul(nn_context* ctx, const nn_mul_job* jobs, uint64_t count);
+/* Tunables: "r_last" (levels of the contiguous NTT pass, 3..12, default 11),
+ * "r_col" (most levels of a strided pass, 1..9, default 9), "batch_ntt_min"
+ * (default 384), "batch_blocks_per_sm" (0 = occupancy limit). */
+nn_status nn_context_set_tunable(nn_context* ctx, const char* name, int64_t value);
+int64_t nn_context_get_tunable(const nn_context* ctx, const char* name);
+
 /* ---- launch accounting (process-wide) ------------------------------------ */
 /* Number of kernels this library has launched since load. */
 uint64_t nn_launch_count(void);

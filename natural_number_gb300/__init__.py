@@ -30,6 +30,12 @@ _vp = C.c_void_p
 _lib = None
 
 
+class MulJob(C.Structure):
+    """nn_mul_job: one product of a batch (device pointers)."""
+    _fields_ = [("d_a", C.c_void_p), ("n_a", C.c_uint64), ("d_b", C.c_void_p), ("n_b", C.c_uint64),
+                ("d_out", C.c_void_p)]
+
+
 class NNError(RuntimeError):
     def __init__(self, status: int, msg: str):
         super().__init__(f"{msg} (status {status})")
@@ -73,6 +79,13 @@ def lib() -> C.CDLL:
         "nn_sqr": (C.c_int, [_vp, _vp, _vp, C.c_uint64]),
         "nn_ntt_mul": (C.c_int, [_vp, _vp, _vp, C.c_uint64, _vp, C.c_uint64, C.c_int, C.c_uint64, _u64p]),
         "nn_mul_base": (C.c_int, [_vp, _vp, _vp, C.c_uint64, _vp, C.c_uint64]),
+        "nn_batch_create": (C.c_int, [_vp, _u64p, _u64p, C.POINTER(C.c_int), C.c_uint64, C.POINTER(_vp)]),
+        "nn_batch_run": (C.c_int, [_vp, _vp, C.POINTER(MulJob)]),
+        "nn_batch_destroy": (C.c_int, [_vp, _vp]),
+        "nn_batch_items": (C.c_uint64, [_vp]),
+        "nn_batch_mul": (C.c_int, [_vp, C.POINTER(MulJob), C.c_uint64]),
+        "nn_context_set_tunable": (C.c_int, [_vp, C.c_char_p, C.c_int64]),
+        "nn_context_get_tunable": (C.c_int64, [_vp, C.c_char_p]),
         "nn_launch_count": (C.c_uint64, []),
         "nn_profile_enable": (None, [C.c_int]),
         "nn_profile_report": (C.c_uint64, [C.c_char_p, C.c_uint64]),
@@ -262,6 +275,61 @@ class Context:
 
     def transform(self) -> "Transform":
         return Transform(self)
+
+    def set_tunable(self, name: str, value: int) -> None:
+        self._check(lib().nn_context_set_tunable(self.h, name.encode(), int(value)), "set_tunable " + name)
+
+    def get_tunable(self, name: str) -> int:
+        return int(lib().nn_context_get_tunable(self.h, name.encode()))
+
+    def batch(self, sizes_a, sizes_b, square=None) -> "Batch":
+        return Batch(self, sizes_a, sizes_b, square)
+
+    def batch_mul_device(self, pairs, outs) -> None:
+        """One-shot batch: pairs of torch tensors (a, b), outputs of n_a + n_b limbs."""
+        arr = (MulJob * len(pairs))()
+        for k, ((a, b), o) in enumerate(zip(pairs, outs)):
+            arr[k] = MulJob(_dptr(a), a.numel(), _dptr(b), b.numel(), _dptr(o))
+        self._check(lib().nn_batch_mul(self.h, arr, len(pairs)), "batch_mul")
+
+
+class Batch:
+    """nn_batch: a planned batch of products (one persistent launch per run,
+    replayed from a CUDA graph)."""
+
+    def __init__(self, ctx: Context, sizes_a, sizes_b, square=None):
+        self.ctx = ctx
+        na = np.ascontiguousarray(sizes_a, dtype=np.uint64)
+        nb = np.ascontiguousarray(sizes_b, dtype=np.uint64)
+        self.count = na.size
+        sq = None
+        if square is not None:
+            self._sq = np.ascontiguousarray(square, dtype=np.int32)
+            sq = self._sq.ctypes.data_as(C.POINTER(C.c_int))
+        h = _vp()
+        ctx._check(lib().nn_batch_create(ctx.h, _ptr(na), _ptr(nb), sq, na.size, C.byref(h)), "batch_create")
+        self.h = h
+        self._jobs = (MulJob * self.count)()
+
+    @property
+    def items(self) -> int:
+        return int(lib().nn_batch_items(self.h))
+
+    def run(self, pairs, outs) -> None:
+        for k, ((a, b), o) in enumerate(zip(pairs, outs)):
+            self._jobs[k] = MulJob(_dptr(a), a.numel(), _dptr(b), b.numel(), _dptr(o))
+        self.ctx._check(lib().nn_batch_run(self.ctx.h, self.h, self._jobs), "batch_run")
+
+    def close(self) -> None:
+        if getattr(self, "h", None) and self.ctx.h:
+            lib().nn_batch_destroy(self.ctx.h, self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Transform:

@@ -137,9 +137,9 @@ cudaError_t batch_configure(int* blocks_per_sm, size_t smem) {
 
 cudaError_t batch_launch(const BatchJob* jobs, const BatchItem* items, u32 n_items, const u32* need, u32* done,
                          u32* head, u32* flags, u32* err, const Tables& t, int grid, size_t smem, cudaStream_t st) {
-  launch_begin("batch_persistent", st);
+  // Recorded into a CUDA graph by the caller, which accounts for the launch
+  // at each replay.
   batch_kernel<<<grid, 256, smem, st>>>(jobs, items, n_items, need, done, head, flags, err, t);
-  launch_end(st);
   return cudaGetLastError();
 }
 

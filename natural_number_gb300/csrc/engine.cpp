@@ -34,6 +34,36 @@ struct nn_context {
   std::string err;
   u64* scratch[3] = {nullptr, nullptr, nullptr};  // grow-only device staging for host calls
   u64 scratch_words[3] = {0, 0, 0};
+  // tunables (nn_context_set_tunable)
+  int r_last = 11;            // levels of the contiguous NTT pass
+  int r_col = 9;              // most levels of a strided column pass
+  u64 batch_ntt_min = 384;    // batches: schoolbook when min(n_a, n_b) is below this
+  int batch_blocks_per_sm = 0;  // persistent CTAs per SM (0: occupancy limit)
+};
+
+struct nn_batch {
+  u64 count = 0;
+  std::vector<u64> na, nb;
+  std::vector<nn::BatchJob> jobs;
+  std::vector<nn::BatchItem> items;
+  std::vector<nn::u32> need;
+  std::vector<u64> off_a, off_b;
+  u64 arena_words = 0;
+  nn::u32 n_ctrs = 0, n_flags = 0;
+  size_t smem = 0;
+  int grid = 0;
+  nn::BatchJob* d_jobs = nullptr;
+  nn::BatchItem* d_items = nullptr;
+  nn::u32* d_need = nullptr;
+  nn::u32* d_state = nullptr;  // done[n_ctrs], head, pad
+  nn::u32* d_flags = nullptr;
+  u64* d_arena = nullptr;
+  u64 dev_words = 0;           // budget accounting of the above
+  nn::BatchJob* h_jobs = nullptr;  // pinned staging of the job table
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t ran = nullptr;
+  bool pending = false;
 };
 
 struct nn_transform {
@@ -109,7 +139,8 @@ nn_status forward(nn_context* c, nn_transform* t, const u64* d_limbs, u64 n, int
   NN_CK(c, nn::tables_ensure(c->tables, s, c->stream), "twiddle tables");
   nn_status st = xform_reserve(c, t, s);
   if (st != NN_OK) return st;
-  NN_CK(c, nn::ntt_forward(d_limbs, n, t->res, s, c->tables, c->stream), "forward NTT");
+  const std::vector<nn::Pass> plan = nn::plan_passes(s, c->r_last, c->r_col);
+  NN_CK(c, nn::ntt_forward(d_limbs, n, t->res, s, c->tables, c->stream, &plan), "forward NTT");
   return NN_OK;
 }
 
@@ -118,7 +149,8 @@ nn_status inverse_save(nn_context* c, nn_transform* t, u64* d_out, u64 size, u64
     c->err = "save: size must be at least 2";
     return NN_ERR_INVALID;
   }
-  NN_CK(c, nn::ntt_inverse(t->res, t->scale, c->tables, c->stream), "inverse NTT");
+  const std::vector<nn::Pass> plan = nn::plan_passes(t->scale, c->r_last, c->r_col);
+  NN_CK(c, nn::ntt_inverse(t->res, t->scale, c->tables, c->stream, &plan), "inverse NTT");
   u64 w = 0;
   NN_CK(c, nn::ntt_save(t->res, t->scale, d_out, size, c->scan, &w, c->stream), "CRT/carry");
   if (written) *written = w;
@@ -223,6 +255,177 @@ nn_status scratch(nn_context* c, int slot, u64 words, u64** p) {
   }
   *p = c->scratch[slot];
   return NN_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batches: a work queue over all jobs' pipeline steps (batch.cu).
+// ---------------------------------------------------------------------------
+constexpr u64 kPointwiseChunk = 1024;
+
+nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, const int* square, u64 count) {
+  B->count = count;
+  B->na.assign(na, na + count);
+  B->nb.assign(nb, nb + count);
+  B->jobs.resize(count);
+  B->off_a.assign(count, 0);
+  B->off_b.assign(count, 0);
+  std::vector<int> steps(count, 0);
+  int max_s = 2;
+  size_t smem = 8;
+  for (u64 j = 0; j < count; ++j) {
+    if (!na[j] || !nb[j]) {
+      c->err = "batch: empty operand";
+      return NN_ERR_INVALID;
+    }
+    nn::BatchJob& J = B->jobs[j];
+    J = nn::BatchJob{};
+    J.na = na[j];
+    J.nb = nb[j];
+    J.ctr_base = B->n_ctrs;
+    J.flag_base = B->n_flags;
+    B->n_flags += (nn::u32)nn::scan_tiles(na[j] + nb[j]);
+    if (std::min(na[j], nb[j]) < c->batch_ntt_min) {
+      J.s = 0;
+      steps[j] = 1;
+    } else {
+      const int s = ntt_scale(na[j], nb[j]);
+      J.s = s;
+      J.square = square ? square[j] : 0;
+      if (J.square && na[j] != nb[j]) {
+        c->err = "batch: a square needs equal operand sizes";
+        return NN_ERR_INVALID;
+      }
+      max_s = std::max(max_s, s);
+      const std::vector<nn::Pass> plan = nn::plan_passes(s, c->r_last, c->r_col);
+      if (plan.size() > 4) {
+        c->err = "batch: transform too long for one batch";
+        return NN_ERR_INVALID;
+      }
+      J.n_pass = (int)plan.size();
+      for (int k = 0; k < J.n_pass; ++k) {
+        J.lambda0[k] = plan[k].lambda0;
+        J.R[k] = plan[k].R;
+        J.C[k] = plan[k].C;
+        smem = std::max(smem, (size_t)plan[k].C << plan[k].R << 3);
+      }
+      steps[j] = 2 * J.n_pass + 2;
+      B->off_a[j] = B->arena_words;
+      B->arena_words += 3ull << s;
+      if (!J.square) {
+        B->off_b[j] = B->arena_words;
+        B->arena_words += 3ull << s;
+      }
+    }
+    B->n_ctrs += steps[j];
+  }
+  B->need.assign(B->n_ctrs, 0);
+  const int max_steps = *std::max_element(steps.begin(), steps.end());
+  B->items.clear();
+  for (int st = 0; st < max_steps; ++st) {
+    for (u64 j = 0; j < count; ++j) {
+      if (st >= steps[j]) continue;
+      const nn::BatchJob& J = B->jobs[j];
+      auto push = [&](unsigned char kind, int pass, int prime, int operand, u64 tile) {
+        nn::BatchItem it{};
+        it.job = (nn::u32)j;
+        it.step = (unsigned short)st;
+        it.kind = kind;
+        it.pass = (unsigned char)pass;
+        it.prime = (unsigned char)prime;
+        it.operand = (unsigned char)operand;
+        it.tile = (nn::u32)tile;
+        B->items.push_back(it);
+        B->need[J.ctr_base + st] += 1;
+      };
+      if (J.s == 0) {
+        for (u64 t = 0; t < nn::scan_tiles(J.na + J.nb); ++t) push(nn::kItemColumn, 0, 0, 0, t);
+        continue;
+      }
+      const int m = J.n_pass;
+      const u64 L = 1ull << J.s;
+      if (st < m) {  // forward pass st of each operand
+        const u64 tiles = L / ((u64)J.C[st] << J.R[st]);
+        for (int op = 0; op < (J.square ? 1 : 2); ++op)
+          for (int pr = 0; pr < 3; ++pr)
+            for (u64 t = 0; t < tiles; ++t) push(nn::kItemFwd, st, pr, op, t);
+      } else if (st == m) {
+        const u64 chunks = (L / 4 + kPointwiseChunk - 1) / kPointwiseChunk;
+        for (int pr = 0; pr < 3; ++pr)
+          for (u64 t = 0; t < chunks; ++t) push(nn::kItemPointwise, 0, pr, 0, t);
+      } else if (st < 2 * m + 1) {  // inverse passes m-1 .. 0
+        const int k = 2 * m - st;
+        const u64 tiles = L / ((u64)J.C[k] << J.R[k]);
+        for (int pr = 0; pr < 3; ++pr)
+          for (u64 t = 0; t < tiles; ++t) push(nn::kItemInv, k, pr, 0, t);
+      } else {
+        for (u64 t = 0; t < nn::scan_tiles(J.na + J.nb); ++t) push(nn::kItemCrt, 0, 0, 0, t);
+      }
+    }
+  }
+  if (B->items.size() >= 0xffffffffull) {
+    c->err = "batch: too many work items";
+    return NN_ERR_INVALID;
+  }
+  B->smem = smem;
+  NN_CK(c, nn::tables_ensure(c->tables, max_s, c->stream), "twiddle tables");
+  int per_sm = 0;
+  NN_CK(c, nn::batch_configure(&per_sm, smem), "batch kernel attributes");
+  if (c->batch_blocks_per_sm > 0) per_sm = std::min(per_sm, c->batch_blocks_per_sm);
+  int sms = 0;
+  NN_CK(c, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device), "device attributes");
+  B->grid = std::max(1, per_sm) * sms;
+  // device tables
+  // Regions in one allocation, each rounded to 256 bytes: the residues are
+  // read and written with 16-byte vector accesses.
+  auto words = [](u64 bytes) { return (bytes + 255) / 256 * 32; };
+  const u64 w_jobs = words(count * sizeof(nn::BatchJob)), w_items = words(B->items.size() * sizeof(nn::BatchItem));
+  const u64 w_need = words(4ull * B->n_ctrs), w_state = words(4ull * (B->n_ctrs + 4)),
+            w_flags = words(4ull * (B->n_flags + 2));
+  u64* p = nullptr;
+  B->dev_words = w_jobs + w_items + w_need + w_state + w_flags + B->arena_words;
+  nn_status st = dev_alloc(c, &p, B->dev_words);
+  if (st != NN_OK) return st;
+  B->d_jobs = reinterpret_cast<nn::BatchJob*>(p);
+  B->d_items = reinterpret_cast<nn::BatchItem*>(p + w_jobs);
+  B->d_need = reinterpret_cast<nn::u32*>(p + w_jobs + w_items);
+  B->d_state = reinterpret_cast<nn::u32*>(p + w_jobs + w_items + w_need);
+  B->d_flags = reinterpret_cast<nn::u32*>(p + w_jobs + w_items + w_need + w_state);
+  B->d_arena = p + w_jobs + w_items + w_need + w_state + w_flags;
+  NN_CK(c, cudaMemcpyAsync(B->d_items, B->items.data(), B->items.size() * sizeof(nn::BatchItem),
+                           cudaMemcpyHostToDevice, c->stream), "upload items");
+  NN_CK(c, cudaMemcpyAsync(B->d_need, B->need.data(), B->need.size() * 4, cudaMemcpyHostToDevice, c->stream),
+        "upload counts");
+  NN_CK(c, cudaHostAlloc((void**)&B->h_jobs, count * sizeof(nn::BatchJob), cudaHostAllocDefault), "pinned jobs");
+  NN_CK(c, cudaEventCreateWithFlags(&B->ran, cudaEventDisableTiming), "event");
+  NN_CK(c, cudaStreamSynchronize(c->stream), "batch plan upload");
+  return NN_OK;
+}
+
+// Records the run sequence (job table upload, counter resets, persistent
+// kernel) into a CUDA graph on the context's own stream.
+nn_status batch_capture(nn_context* c, nn_batch* B) {
+  cudaStream_t cs = c->own;
+  NN_CK(c, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "begin capture");
+  cudaMemcpyAsync(B->d_jobs, B->h_jobs, B->count * sizeof(nn::BatchJob), cudaMemcpyHostToDevice, cs);
+  cudaMemsetAsync(B->d_state, 0, (B->n_ctrs + 4) * 4, cs);
+  cudaMemsetAsync(B->d_flags, 0, (B->n_flags + 2) * 4, cs);
+  cudaError_t le = nn::batch_launch(B->d_jobs, B->d_items, (nn::u32)B->items.size(), B->d_need, B->d_state,
+                                    B->d_state + B->n_ctrs, B->d_flags, c->scan.err, c->tables, B->grid, B->smem, cs);
+  cudaError_t e = cudaStreamEndCapture(cs, &B->graph);
+  if (le != cudaSuccess) return fail(c, le, "batch launch (capture)");
+  NN_CK(c, e, "end capture");
+  NN_CK(c, cudaGraphInstantiate(&B->exec, B->graph, 0), "graph instantiate");
+  return NN_OK;
+}
+
+void batch_release(nn_context* c, nn_batch* B) {
+  if (B->pending) cudaEventSynchronize(B->ran);
+  if (B->exec) cudaGraphExecDestroy(B->exec);
+  if (B->graph) cudaGraphDestroy(B->graph);
+  if (B->ran) cudaEventDestroy(B->ran);
+  if (B->h_jobs) cudaFreeHost(B->h_jobs);
+  dev_free(c, reinterpret_cast<u64*>(B->d_jobs), B->dev_words);
+  delete B;
 }
 
 u64 normalized(const u64* x, u64 n) {  // natural::std (natural.h:82-93)
@@ -477,6 +680,102 @@ nn_status nn_transform_inverse_save_host(nn_context* c, nn_transform* t, uint64_
   NN_CK(c, cudaMemcpyAsync(out, d, w * 8, cudaMemcpyDeviceToHost, c->stream), "D2H");
   st = nn_context_synchronize(c);
   if (written) *written = w;
+  return st;
+}
+
+nn_status nn_context_set_tunable(nn_context* c, const char* name, int64_t v) {
+  if (!c || !name) return NN_ERR_INVALID;
+  std::string k(name);
+  if (k == "r_last" && v >= 3 && v <= 12)
+    c->r_last = (int)v;
+  else if (k == "r_col" && v >= 1 && v <= 9)
+    c->r_col = (int)v;
+  else if (k == "batch_ntt_min" && v >= 1)
+    c->batch_ntt_min = (u64)v;
+  else if (k == "batch_blocks_per_sm" && v >= 0 && v <= 32)
+    c->batch_blocks_per_sm = (int)v;
+  else {
+    c->err = "unknown tunable or value out of range: " + k;
+    return NN_ERR_INVALID;
+  }
+  return NN_OK;
+}
+
+int64_t nn_context_get_tunable(const nn_context* c, const char* name) {
+  if (!c || !name) return -1;
+  std::string k(name);
+  if (k == "r_last") return c->r_last;
+  if (k == "r_col") return c->r_col;
+  if (k == "batch_ntt_min") return (int64_t)c->batch_ntt_min;
+  if (k == "batch_blocks_per_sm") return c->batch_blocks_per_sm;
+  return -1;
+}
+
+nn_status nn_batch_create(nn_context* c, const uint64_t* na, const uint64_t* nb, const int* square, uint64_t count,
+                          nn_batch** out) {
+  if (!c || !na || !nb || !count || !out) return NN_ERR_INVALID;
+  *out = nullptr;
+  nn_batch* B = new nn_batch;
+  nn_status st = batch_plan(c, B, na, nb, square, count);
+  if (st != NN_OK) {
+    batch_release(c, B);
+    return st;
+  }
+  *out = B;
+  return NN_OK;
+}
+
+nn_status nn_batch_run(nn_context* c, nn_batch* B, const nn_mul_job* jobs) {
+  if (!c || !B || !jobs) return NN_ERR_INVALID;
+  if (B->pending) NN_CK(c, cudaEventSynchronize(B->ran), "previous batch run");
+  for (u64 j = 0; j < B->count; ++j) {
+    if (jobs[j].n_a != B->na[j] || jobs[j].n_b != B->nb[j] || !jobs[j].d_a || !jobs[j].d_b || !jobs[j].d_out) {
+      c->err = "batch run: job does not match the plan";
+      return NN_ERR_INVALID;
+    }
+    nn::BatchJob J = B->jobs[j];
+    J.a = jobs[j].d_a;
+    J.b = jobs[j].d_b;
+    J.out = jobs[j].d_out;
+    J.res_a = B->d_arena + B->off_a[j];
+    J.res_b = B->d_arena + B->off_b[j];
+    B->h_jobs[j] = J;
+  }
+  if (!B->exec) {
+    nn_status st = batch_capture(c, B);
+    if (st != NN_OK) return st;
+  }
+  nn::launch_begin("batch_persistent", c->stream);
+  cudaError_t ge = cudaGraphLaunch(B->exec, c->stream);
+  nn::launch_end(c->stream);
+  NN_CK(c, ge, "graph launch");
+  NN_CK(c, cudaEventRecord(B->ran, c->stream), "event record");
+  B->pending = true;
+  return NN_OK;
+}
+
+nn_status nn_batch_destroy(nn_context* c, nn_batch* B) {
+  if (!c || !B) return NN_ERR_INVALID;
+  batch_release(c, B);
+  return NN_OK;
+}
+
+uint64_t nn_batch_items(const nn_batch* B) { return B ? B->items.size() : 0; }
+
+nn_status nn_batch_mul(nn_context* c, const nn_mul_job* jobs, uint64_t count) {
+  if (!c || !jobs || !count) return NN_ERR_INVALID;
+  std::vector<u64> na(count), nb(count);
+  std::vector<int> sq(count);
+  for (u64 j = 0; j < count; ++j) {
+    na[j] = jobs[j].n_a;
+    nb[j] = jobs[j].n_b;
+    sq[j] = jobs[j].d_a == jobs[j].d_b && na[j] == nb[j];
+  }
+  nn_batch* B = nullptr;
+  nn_status st = nn_batch_create(c, na.data(), nb.data(), sq.data(), count, &B);
+  if (st != NN_OK) return st;
+  st = nn_batch_run(c, B, jobs);
+  batch_release(c, B);
   return st;
 }
 

@@ -1,0 +1,76 @@
+"""Batched products (one persistent launch over a work queue) against the
+oracle: mixed sizes on both sides of the schoolbook/NTT switch, squares,
+repeated runs of one plan (CUDA-graph replay) with new operands."""
+import numpy as np
+import pytest
+
+from gpu_util import empty_dev, normalize, to_dev, to_host
+from natural_number_gb300.synth import limbs, log_uniform_sizes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import natural_number_gb300 as nn
+    c = nn.Context(0)
+    yield c
+    c.close()
+
+
+def run_batch(ctx, a_list, b_list, square=None, plan=None):
+    import torch
+    da = [to_dev(a) for a in a_list]
+    db = [da[k] if (square is not None and square[k]) else to_dev(b) for k, b in enumerate(b_list)]
+    outs = [empty_dev(a.size + b.size) for a, b in zip(a_list, b_list)]
+    if plan is None:
+        plan = ctx.batch([a.size for a in a_list], [b.size for b in b_list], square)
+    plan.run(list(zip(da, db)), outs)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    return [to_host(o) for o in outs], plan
+
+
+def test_batch_mixed_sizes_vs_oracle(ctx, oracle):
+    n = 160
+    sa = log_uniform_sizes(11, n, 1, 14)
+    sb = log_uniform_sizes(12, n, 1, 14)
+    a_list = [limbs(100 + k, int(x)) for k, x in enumerate(sa)]
+    b_list = [limbs(900 + k, int(x)) for k, x in enumerate(sb)]
+    outs, plan = run_batch(ctx, a_list, b_list)
+    for k in range(n):
+        assert np.array_equal(normalize(outs[k]), oracle.mul(a_list[k], b_list[k])), (k, sa[k], sb[k])
+    assert plan.items > n
+
+
+def test_batch_replay_with_new_operands(ctx, oracle):
+    sizes = [(64, 64), (383, 4000), (384, 384), (5000, 3000), (20000, 20001), (1, 7), (70000, 1000)]
+    a1 = [limbs(k + 1, x) for k, (x, _) in enumerate(sizes)]
+    b1 = [limbs(k + 50, y) for k, (_, y) in enumerate(sizes)]
+    outs, plan = run_batch(ctx, a1, b1)
+    for k in range(len(sizes)):
+        assert np.array_equal(normalize(outs[k]), oracle.mul(a1[k], b1[k]))
+    a2 = [np.full(x, 2**64 - 1, dtype=np.uint64) for x, _ in sizes]
+    b2 = [limbs(k + 500, y) for k, (_, y) in enumerate(sizes)]
+    for _ in range(2):
+        outs, _ = run_batch(ctx, a2, b2, plan=plan)
+        for k in range(len(sizes)):
+            assert np.array_equal(normalize(outs[k]), normalize(oracle.mul(a2[k], b2[k])))
+
+
+def test_batch_squares_and_threshold_tunable(ctx, oracle):
+    sizes = [300, 384, 1000, 4096, 9000]
+    a_list = [limbs(k + 7, x) for k, x in enumerate(sizes)]
+    outs, _ = run_batch(ctx, a_list, a_list, square=[1] * len(sizes))
+    for k, a in enumerate(a_list):
+        assert np.array_equal(normalize(outs[k]), oracle.sqr(a))
+    old = ctx.get_tunable("batch_ntt_min")
+    try:
+        ctx.set_tunable("batch_ntt_min", 64)  # push mid sizes onto the NTT route
+        a_list = [limbs(k + 70, x) for k, x in enumerate([64, 100, 200, 383])]
+        b_list = [limbs(k + 80, x) for k, x in enumerate([70, 100, 250, 383])]
+        outs, _ = run_batch(ctx, a_list, b_list)
+        for k in range(4):
+            assert np.array_equal(normalize(outs[k]), oracle.mul(a_list[k], b_list[k]))
+    finally:
+        ctx.set_tunable("batch_ntt_min", old)
