@@ -138,6 +138,51 @@ class ClockSampler:
                 "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit())}
 
 
+def measure_batched(ctx, steps: int, warmup: int, count: int = 4096) -> dict:
+    """Uneven-size batch: `count` products with operand lengths drawn
+    independently log-uniform in [2^6, 2^18] limbs, once one nn_mul per
+    product (the unbatched path, run from a C loop) and once as one planned
+    batch (persistent work-queue launch replayed from a CUDA graph); both on
+    the same device-resident operands, timed with CUDA events, results compared."""
+    import torch
+
+    from natural_number_gb300.workloads import UnevenProducts
+    W = UnevenProducts(count)
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    ctx.mul_each(W.jobs_plain)
+    plain_ms = timed(lambda: ctx.mul_each(W.jobs_plain), max(2, steps // 3))
+    t0 = time.perf_counter()
+    plan = ctx.batch(W.sa, W.sb)
+    plan_s = time.perf_counter() - t0
+    for _ in range(max(warmup, 1)):
+        plan.run_jobs(W.jobs_batch)
+    batch_ms = timed(lambda: plan.run_jobs(W.jobs_batch), steps)
+    ctx.synchronize()
+    identical = bool(torch.equal(W.out_plain, W.out_batch))
+    out = {"workload": "%d products, operand lengths log-uniform in [2^6, 2^18] limbs (independent), "
+                       "%d product limbs in total, %.0f%% of products on the NTT route"
+                       % (count, W.limbs_total, 100 * W.ntt_fraction(ctx.get_tunable("batch_ntt_min"))),
+           "plain_ms": plain_ms, "batched_ms": batch_ms,
+           "plain_limbs_per_s": W.limbs_total / (plain_ms / 1e3),
+           "batched_limbs_per_s": W.limbs_total / (batch_ms / 1e3),
+           "speedup": plain_ms / batch_ms, "identical": identical, "work_items": plan.items,
+           "plan_seconds": plan_s}
+    plan.close()
+    del W
+    return out
+
+
 def cpu_baseline_port() -> dict:
     """The oracle (single-threaded CPU restatement) on one 2^24 x 2^24 product."""
     from natural_number_gb300.synth import limbs
@@ -202,6 +247,7 @@ def main() -> None:
     ap.add_argument("--n-exp", type=int, default=N_EXP, help="operand size 2^n limbs (27 = the benchmark workload)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the uneven-size batch measurement")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -287,6 +333,10 @@ def main() -> None:
         e2e = {"value": world * 2 * n / (e_ms / 1e3), "unit": UNIT, "ms_per_step": e_ms,
                "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 16 * n}
 
+    batched = None
+    if not args.no_batch:
+        batched = measure_batched(ctx, args.steps, args.warmup)
+
     if rank != 0:
         return
     peak, peak_kind = peaks()
@@ -318,6 +368,8 @@ def main() -> None:
     }
     if e2e:
         line["e2e"] = e2e
+    if batched:
+        line["batched"] = batched
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_port()
     print(json.dumps(line))

@@ -115,11 +115,15 @@ nn_status nn_batch_create(nn_context* ctx, const uint64_t* n_a, const uint64_t* 
 nn_status nn_batch_run(nn_context* ctx, nn_batch* batch, const nn_mul_job* jobs);
 nn_status nn_batch_destroy(nn_context* ctx, nn_batch* batch);
 uint64_t nn_batch_items(const nn_batch* batch);
+/* The same products one nn_mul at a time (one launch sequence per product):
+ * the unbatched path, for comparison. */
+nn_status nn_mul_each(nn_context* ctx, const nn_mul_job* jobs, uint64_t count);
 /* Plan + run + release in one call. */
 nn_status nn_batch_mul(nn_context* ctx, const nn_mul_job* jobs, uint64_t count);
 /* Tunables: "r_last" (levels of the contiguous NTT pass, 3..12, default 11),
- * "r_col" (most levels of a strided pass, 1..9, default 9), "batch_ntt_min"
- * (default 384), "batch_blocks_per_sm" (0 = occupancy limit). */
+ * "r_col" (most levels of a strided pass, 1..9, default 9), "r_last@<s>" and
+ * "r_col@<s>" (the same for transforms of scale s only; 0 = default),
+ * "batch_ntt_min" (default 384), "batch_blocks_per_sm" (0 = occupancy limit). */
 nn_status nn_context_set_tunable(nn_context* ctx, const char* name, int64_t value);
 int64_t nn_context_get_tunable(const nn_context* ctx, const char* name);
 

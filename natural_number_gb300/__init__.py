@@ -84,6 +84,7 @@ def lib() -> C.CDLL:
         "nn_batch_destroy": (C.c_int, [_vp, _vp]),
         "nn_batch_items": (C.c_uint64, [_vp]),
         "nn_batch_mul": (C.c_int, [_vp, C.POINTER(MulJob), C.c_uint64]),
+        "nn_mul_each": (C.c_int, [_vp, C.POINTER(MulJob), C.c_uint64]),
         "nn_context_set_tunable": (C.c_int, [_vp, C.c_char_p, C.c_int64]),
         "nn_context_get_tunable": (C.c_int64, [_vp, C.c_char_p]),
         "nn_launch_count": (C.c_uint64, []),
@@ -138,6 +139,8 @@ class Context:
             raise NNError(st, "nn_context_create: " + L.nn_status_string(st).decode())
         self.h = h
         self.device = device
+        from .autotune import apply as _apply_tuning
+        self.tuning = _apply_tuning(self)
         if use_torch_stream:
             try:
                 import torch
@@ -282,6 +285,10 @@ class Context:
     def get_tunable(self, name: str) -> int:
         return int(lib().nn_context_get_tunable(self.h, name.encode()))
 
+    def mul_each(self, jobs) -> None:
+        """Products one nn_mul at a time from a MulJob array (unbatched path)."""
+        self._check(lib().nn_mul_each(self.h, jobs, len(jobs)), "mul_each")
+
     def batch(self, sizes_a, sizes_b, square=None) -> "Batch":
         return Batch(self, sizes_a, sizes_b, square)
 
@@ -319,6 +326,10 @@ class Batch:
         for k, ((a, b), o) in enumerate(zip(pairs, outs)):
             self._jobs[k] = MulJob(_dptr(a), a.numel(), _dptr(b), b.numel(), _dptr(o))
         self.ctx._check(lib().nn_batch_run(self.ctx.h, self.h, self._jobs), "batch_run")
+
+    def run_jobs(self, jobs) -> None:
+        """Runs on a prepared MulJob array (no per-job Python work)."""
+        self.ctx._check(lib().nn_batch_run(self.ctx.h, self.h, jobs), "batch_run")
 
     def close(self) -> None:
         if getattr(self, "h", None) and self.ctx.h:

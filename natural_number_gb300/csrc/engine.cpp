@@ -37,6 +37,13 @@ struct nn_context {
   // tunables (nn_context_set_tunable)
   int r_last = 11;            // levels of the contiguous NTT pass
   int r_col = 9;              // most levels of a strided column pass
+  int r_last_at[64] = {};     // per-scale overrides (0: use r_last / r_col)
+  int r_col_at[64] = {};
+  std::vector<nn::Pass> passes(int s) const {
+    const int rl = (s >= 0 && s < 64 && r_last_at[s]) ? r_last_at[s] : r_last;
+    const int rc = (s >= 0 && s < 64 && r_col_at[s]) ? r_col_at[s] : r_col;
+    return nn::plan_passes(s, rl, rc);
+  }
   u64 batch_ntt_min = 384;    // batches: schoolbook when min(n_a, n_b) is below this
   int batch_blocks_per_sm = 0;  // persistent CTAs per SM (0: occupancy limit)
 };
@@ -139,7 +146,7 @@ nn_status forward(nn_context* c, nn_transform* t, const u64* d_limbs, u64 n, int
   NN_CK(c, nn::tables_ensure(c->tables, s, c->stream), "twiddle tables");
   nn_status st = xform_reserve(c, t, s);
   if (st != NN_OK) return st;
-  const std::vector<nn::Pass> plan = nn::plan_passes(s, c->r_last, c->r_col);
+  const std::vector<nn::Pass> plan = c->passes(s);
   NN_CK(c, nn::ntt_forward(d_limbs, n, t->res, s, c->tables, c->stream, &plan), "forward NTT");
   return NN_OK;
 }
@@ -149,7 +156,7 @@ nn_status inverse_save(nn_context* c, nn_transform* t, u64* d_out, u64 size, u64
     c->err = "save: size must be at least 2";
     return NN_ERR_INVALID;
   }
-  const std::vector<nn::Pass> plan = nn::plan_passes(t->scale, c->r_last, c->r_col);
+  const std::vector<nn::Pass> plan = c->passes(t->scale);
   NN_CK(c, nn::ntt_inverse(t->res, t->scale, c->tables, c->stream, &plan), "inverse NTT");
   u64 w = 0;
   NN_CK(c, nn::ntt_save(t->res, t->scale, d_out, size, c->scan, &w, c->stream), "CRT/carry");
@@ -296,7 +303,7 @@ nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, c
         return NN_ERR_INVALID;
       }
       max_s = std::max(max_s, s);
-      const std::vector<nn::Pass> plan = nn::plan_passes(s, c->r_last, c->r_col);
+      const std::vector<nn::Pass> plan = c->passes(s);
       if (plan.size() > 4) {
         c->err = "batch: transform too long for one batch";
         return NN_ERR_INVALID;
@@ -686,6 +693,18 @@ nn_status nn_transform_inverse_save_host(nn_context* c, nn_transform* t, uint64_
 nn_status nn_context_set_tunable(nn_context* c, const char* name, int64_t v) {
   if (!c || !name) return NN_ERR_INVALID;
   std::string k(name);
+  const size_t at = k.find('@');
+  if (at != std::string::npos) {  // per-scale pass split: "r_last@28", "r_col@28"
+    const std::string base = k.substr(0, at);
+    const int sc = std::atoi(k.c_str() + at + 1);
+    if (sc >= 2 && sc < 64 && ((base == "r_last" && (v == 0 || (v >= 3 && v <= 12))) ||
+                               (base == "r_col" && v >= 0 && v <= 9))) {
+      (base == "r_last" ? c->r_last_at : c->r_col_at)[sc] = (int)v;
+      return NN_OK;
+    }
+    c->err = "unknown tunable or value out of range: " + k;
+    return NN_ERR_INVALID;
+  }
   if (k == "r_last" && v >= 3 && v <= 12)
     c->r_last = (int)v;
   else if (k == "r_col" && v >= 1 && v <= 9)
@@ -704,6 +723,14 @@ nn_status nn_context_set_tunable(nn_context* c, const char* name, int64_t v) {
 int64_t nn_context_get_tunable(const nn_context* c, const char* name) {
   if (!c || !name) return -1;
   std::string k(name);
+  const size_t at = k.find('@');
+  if (at != std::string::npos) {
+    const int sc = std::atoi(k.c_str() + at + 1);
+    if (sc < 2 || sc >= 64) return -1;
+    if (k.substr(0, at) == "r_last") return c->r_last_at[sc];
+    if (k.substr(0, at) == "r_col") return c->r_col_at[sc];
+    return -1;
+  }
   if (k == "r_last") return c->r_last;
   if (k == "r_col") return c->r_col;
   if (k == "batch_ntt_min") return (int64_t)c->batch_ntt_min;
@@ -761,6 +788,15 @@ nn_status nn_batch_destroy(nn_context* c, nn_batch* B) {
 }
 
 uint64_t nn_batch_items(const nn_batch* B) { return B ? B->items.size() : 0; }
+
+nn_status nn_mul_each(nn_context* c, const nn_mul_job* jobs, uint64_t count) {
+  if (!c || !jobs) return NN_ERR_INVALID;
+  for (u64 j = 0; j < count; ++j) {
+    nn_status st = mul_impl(c, jobs[j].d_out, jobs[j].d_a, jobs[j].n_a, jobs[j].d_b, jobs[j].n_b);
+    if (st != NN_OK) return st;
+  }
+  return NN_OK;
+}
 
 nn_status nn_batch_mul(nn_context* c, const nn_mul_job* jobs, uint64_t count) {
   if (!c || !jobs || !count) return NN_ERR_INVALID;
