@@ -127,6 +127,22 @@ nn_status nn_batch_mul(nn_context* ctx, const nn_mul_job* jobs, uint64_t count);
 nn_status nn_context_set_tunable(nn_context* ctx, const char* name, int64_t value);
 int64_t nn_context_get_tunable(const nn_context* ctx, const char* name);
 
+/* ---- allocation-free schoolbook product ---------------------------------- */
+/* No counterpart in the reference.  For callers that must not allocate device
+ * memory where they multiply: code running under another framework's memory
+ * pool, or latency-sensitive loops where cudaMalloc/cudaFree would stall the
+ * device.  Same product as nn_mul_base (d_out: n_a + n_b limbs, not
+ * normalised), ordered on `stream` (a cudaStream_t; NULL = default stream),
+ * without a context and without any allocation: the carry scan's status words
+ * live in a fixed device array of the library, sized for n_a + n_b <= 2^22
+ * limbs (larger products return NN_ERR_INVALID).  The first call on a device
+ * looks up that array's device address (cudaGetSymbolAddress) with the device
+ * current; make that first call before any stream capture.  Every call shares
+ * the one array and clears what it needs, so calls that overlap on the GPU
+ * (different streams, or devices sharing none of this) race: order them. */
+nn_status nn_mul_base_noalloc(const uint64_t* d_a, uint64_t n_a, const uint64_t* d_b, uint64_t n_b,
+                              uint64_t* d_out, void* stream);
+
 /* ---- launch accounting (process-wide) ------------------------------------ */
 /* Number of kernels this library has launched since load. */
 uint64_t nn_launch_count(void);

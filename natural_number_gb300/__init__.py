@@ -87,6 +87,7 @@ def lib() -> C.CDLL:
         "nn_mul_each": (C.c_int, [_vp, C.POINTER(MulJob), C.c_uint64]),
         "nn_context_set_tunable": (C.c_int, [_vp, C.c_char_p, C.c_int64]),
         "nn_context_get_tunable": (C.c_int64, [_vp, C.c_char_p]),
+        "nn_mul_base_noalloc": (C.c_int, [_vp, C.c_uint64, _vp, C.c_uint64, _vp, _vp]),
         "nn_launch_count": (C.c_uint64, []),
         "nn_profile_enable": (None, [C.c_int]),
         "nn_profile_report": (C.c_uint64, [C.c_char_p, C.c_uint64]),
