@@ -50,8 +50,8 @@ def kernel_bytes(name: str, na: int, nb: int, L: int) -> float:
         return 4.0 * (na + nb) + 24.0 * L  # mean operand length: one launch per operand
     if name.startswith("ntt_fwd_") or name.startswith("ntt_inv_"):
         return 48.0 * L
-    if name == "ntt_pointwise":
-        return 72.0 * L
+    if name in ("ntt_pointwise", "ntt_fused_row_pass"):
+        return 72.0 * L  # fused: reads both transforms, writes one
     if name == "crt_carry_scan":
         return 24.0 * L + 8.0 * (na + nb)
     return 0.0
@@ -248,6 +248,8 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the uneven-size batch measurement")
+    ap.add_argument("--no-serve", action="store_true", help="skip the served request stream")
+    ap.add_argument("--serve-jobs", type=int, default=300)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -336,6 +338,10 @@ def main() -> None:
     batched = None
     if not args.no_batch:
         batched = measure_batched(ctx, args.steps, args.warmup)
+    serving = None
+    if not args.no_serve and rank == 0:
+        from natural_number_gb300 import serving as serving_mod
+        serving = serving_mod.measure(args.serve_jobs)
 
     if rank != 0:
         return
@@ -370,6 +376,8 @@ def main() -> None:
         line["e2e"] = e2e
     if batched:
         line["batched"] = batched
+    if serving:
+        line["serving"] = serving
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_port()
     print(json.dumps(line))

@@ -113,6 +113,10 @@ nn_status nn_batch_create(nn_context* ctx, const uint64_t* n_a, const uint64_t* 
                           uint64_t count, nn_batch** out);
 /* Runs the planned batch on these operands (sizes must match the plan). */
 nn_status nn_batch_run(nn_context* ctx, nn_batch* batch, const nn_mul_job* jobs);
+/* As nn_batch_run, but launched directly rather than from the CUDA graph
+ * (for plans that run once). */
+nn_status nn_batch_launch(nn_context* ctx, nn_batch* batch, const nn_mul_job* jobs);
+/* Releases a plan; waits for its last run to finish first. */
 nn_status nn_batch_destroy(nn_context* ctx, nn_batch* batch);
 uint64_t nn_batch_items(const nn_batch* batch);
 /* The same products one nn_mul at a time (one launch sequence per product):
@@ -142,6 +146,39 @@ int64_t nn_context_get_tunable(const nn_context* ctx, const char* name);
  * (different streams, or devices sharing none of this) race: order them. */
 nn_status nn_mul_base_noalloc(const uint64_t* d_a, uint64_t n_a, const uint64_t* d_b, uint64_t n_b,
                               uint64_t* d_out, void* stream);
+
+/* ---- serving: continuous batching of multiply/divide requests ------------ */
+/* No counterpart in the reference (which has no server).  Requests on host
+ * memory are admitted in arrival order while their estimated device footprint
+ * fits hbm_budget (0: no budget); each scheduler pass launches the newly
+ * admitted products as one batch on the next of `streams` streams, so batches
+ * of later arrivals overlap earlier ones on the device; divisions
+ * (natural::_div, natural.h:749-769) run on `div_workers` threads with their
+ * own contexts.  Operands stay on the device from admission to completion.
+ * Host buffers must stay valid until the request is waited for. */
+typedef struct nn_server nn_server;
+typedef struct {
+  nn_status status;
+  uint64_t out_n;     /* product limbs (normalised) or quotient limbs */
+  uint64_t r_n;       /* remainder limbs (division) */
+  double t_submit, t_admit, t_done;  /* seconds on the server's clock */
+} nn_request_info;
+typedef struct {
+  uint64_t in_flight_bytes, peak_bytes, waiting, batches, max_concurrent_batches, max_batch_jobs;
+} nn_server_stats;
+nn_status nn_server_create(int device, uint64_t hbm_budget, int streams, int div_workers, nn_server** out);
+/* out: n_a + n_b limbs.  A request larger than the whole budget returns NN_ERR_BUDGET. */
+nn_status nn_server_submit_mul(nn_server* s, const uint64_t* a, uint64_t n_a, const uint64_t* b, uint64_t n_b,
+                               uint64_t* out, uint64_t* ticket);
+/* q: n_a + 1 limbs, r: max(n_a, n_b) + 1 limbs (the reference's result sizes fit). */
+nn_status nn_server_submit_div(nn_server* s, const uint64_t* a, uint64_t n_a, const uint64_t* b, uint64_t n_b,
+                               uint64_t* q, uint64_t* r, uint64_t* ticket);
+/* Waits for a request (NN_ERR_TIMEOUT after timeout_s), fills info, forgets the ticket. */
+nn_status nn_server_wait(nn_server* s, uint64_t ticket, double timeout_s, nn_request_info* info);
+nn_status nn_server_get_stats(nn_server* s, nn_server_stats* out);
+double nn_server_clock(nn_server* s);
+/* Finishes every submitted request, then stops. */
+nn_status nn_server_destroy(nn_server* s);
 
 /* ---- launch accounting (process-wide) ------------------------------------ */
 /* Number of kernels this library has launched since load. */

@@ -135,6 +135,12 @@ inline uint64_t div_128(uint64_t lo, uint64_t hi, uint64_t d, uint64_t* rem = nu
   return q;
 }
 
+// Thrown where the reference's Newton division would break one of its own
+// size preconditions (the reference then reads or copies out of bounds and
+// aborts, e.g. for some 2n-by-n-limb divisions); _div then takes the exact
+// Newton division below instead.
+struct precondition_broken {};
+
 constexpr uint64_t NTTmul_threshold = 384;  // ntt_info.h:6
 constexpr uint64_t NTTdiv_threshold = 256;  // ntt_info.h:7
 constexpr int NTTscale_threshold = 10;      // ntt_info.h:8
@@ -595,8 +601,10 @@ inline natural reciprocal(const natural& divs, uint64_t divd_size) {
     if (nxt_acc == NTTdiv_threshold) nxt_acc = NTTdiv_threshold - 1;
     tmp >>= (2 * cur_acc - nxt_acc) << 6;
     if (tmp == 0) tmp = 1;
+    if (nxt_acc < cur_acc) throw precondition_broken();  // natural.h:614 would shift by a negative count
     mul_load_NTT_info(tmp, ans, tmp, ni_ans);
     ans <<= (nxt_acc - cur_acc) << 6;
+    if (tmp.size < cur_acc || tmp.size - cur_acc > ans.size) throw precondition_broken();  // natural.h:615
     add(ans.data, ans.data, ans.size, tmp.data + cur_acc, tmp.size - cur_acc);
   }
 }
@@ -643,7 +651,9 @@ inline natural reciprocal(const natural& divisor, uint64_t dividend_size, NTT_in
     }
     mul_load_NTT_info(tmp, ans, tmp, ni_ans);
     tmp >>= prev_acc << 6;
+    if (cur_acc < prev_acc) throw precondition_broken();  // natural.h:670-672: negative memset length
     const uint64_t inc_acc = cur_acc - prev_acc;
+    if (inc_acc < tmp.size && tmp.size - inc_acc > prev_acc) throw precondition_broken();  // natural.h:676
     const uint64_t have = tmp.size;
     tmp.resize(std::max(cur_acc, have));
     tmp.size = have;
@@ -691,6 +701,7 @@ inline void div_iterative(const natural& divd, const natural& divs, natural& q, 
     tmp >>= rec.size << 6;
     add(q.data + idx, q.data + idx, q.size - idx, tmp.data, tmp.size);
     mul_load_NTT_info(tmp, b, tmp, ni_b);
+    if (r.size < idx || r.size - idx < tmp.size) throw precondition_broken();  // natural.h:724
     sub(r.data + idx, r.data + idx, r.size - idx, tmp.data, tmp.size);
     r.std();
     if (ni_b.NTT_scale) {
@@ -704,12 +715,93 @@ inline void div_iterative(const natural& divd, const natural& divs, natural& q, 
     }
     if (idx == 0) break;
   }
-  while (r >= b) {
+  for (int guard = 0; r >= b; ++guard) {
+    if (guard > 64) throw precondition_broken();  // block estimates are meant to be within a few units
     q += 1;
     r -= b;
   }
   r >>= n_shl;
 }
+
+// Exact Newton division (no counterpart in the reference), for the inputs on
+// which the reference's own division breaks.  With the divisor normalised
+// (top bit set, n limbs), R_k = floor(B^(n+k) / d) is built by recursive
+// doubling: from X = R_h, h = ceil(k/2), and eps = B^(n+h) - d X (< d),
+//   Z = X B^(k-h) + floor(eps X / B^(n+2h-k))
+// underestimates R_k by less than 2, and exact checks against d Z finish it.
+// Then q' = floor(a R_k / B^(n+k)) with k = m - n + 1 is q or q - 1.
+// Every product runs on the GPU; the host adds, shifts and compares.
+namespace nn_gb300 {
+inline natural power_of_B(uint64_t e) {
+  natural p;
+  p.resize(e + 1);
+  std::memset(p.data, 0, 8 * e);
+  p[e] = 1;
+  return p;
+}
+// floor(B^(n+k) / d) for normalised d of n >= 2 limbs.
+inline natural recip_floor(const natural& d, uint64_t k) {
+  const uint64_t n = d.size;
+  if (k == 0) {  // B^n / d lies in (1, 2]
+    natural half = power_of_B(n - 1) << 63;
+    return natural(d == half ? 2 : 1);
+  }
+  if (k == 1) {  // B + floor(B E / d), E = B^n - d < d
+    natural E = power_of_B(n) - d;
+    uint64_t e_hi = E.size == n ? E[n - 1] : 0, e_lo = E.size >= n - 1 ? E[n - 2] : 0;
+    if (E.size < n - 1) e_lo = 0;
+    unsigned __int128 num = ((unsigned __int128)e_hi << 64) | e_lo;
+    uint64_t t = (uint64_t)(num / ((unsigned __int128)d[n - 1] + 1));  // underestimate
+    natural S = (E << 64) - d * natural(t);
+    for (int g = 0; S >= d; ++g) {
+      if (g > 8) throw std::runtime_error("natural_gb300: reciprocal base case did not converge");
+      t += 1;
+      S -= d;
+    }
+    natural Y = power_of_B(1);
+    Y += natural(t);
+    return Y;
+  }
+  const uint64_t h = (k + 1) / 2;
+  natural X = recip_floor(d, h);
+  natural eps = power_of_B(n + h) - d * X;
+  natural Z = (X << (64 * (k - h))) + ((eps * X) >> (64 * (n + 2 * h - k)));
+  natural T = d * Z;
+  const natural top = power_of_B(n + k);
+  for (int g = 0; T > top; ++g) {  // cannot happen: Z underestimates
+    if (g > 8) throw std::runtime_error("natural_gb300: reciprocal overshoot");
+    Z -= 1;
+    T -= d;
+  }
+  natural E = top - T;
+  for (int g = 0; E >= d; ++g) {
+    if (g > 8) throw std::runtime_error("natural_gb300: reciprocal did not converge");
+    Z += 1;
+    E -= d;
+  }
+  return Z;
+}
+// q = floor(a / b), r = a mod b for b of at least two limbs.
+inline void div_newton_exact(const natural& a, const natural& b, natural& q, natural& r) {
+  const unsigned sh = (unsigned)std::countl_zero(b[b.size - 1]);
+  natural d = b << sh, x = a << sh;
+  if (x < d) {
+    q = 0;
+    r = a;
+    return;
+  }
+  const uint64_t n = d.size, k = x.size - n + 1;
+  natural R = recip_floor(d, k);
+  q = (x * R) >> (64 * (n + k));
+  natural rr = x - q * d;  // q <= true quotient, so this is x - q d itself
+  for (int g = 0; rr >= d; ++g) {
+    if (g > 8) throw std::runtime_error("natural_gb300: quotient correction did not converge");
+    q += 1;
+    rr -= d;
+  }
+  r = rr >> sh;
+}
+}  // namespace nn_gb300
 
 inline natural& natural::_div(const natural* ap, const natural* bp, natural* r) {  // natural.h:749-769
   if (*bp == 0) {
@@ -730,7 +822,11 @@ inline natural& natural::_div(const natural* ap, const natural* bp, natural* r) 
     return *this;
   }
   natural a(*ap), b(*bp), q, rr;
-  div_iterative(a, b, q, rr);
+  try {
+    div_iterative(a, b, q, rr);
+  } catch (const nn_gb300::precondition_broken&) {
+    nn_gb300::div_newton_exact(a, b, q, rr);
+  }
   *this = std::move(q);
   *r = std::move(rr);
   return *this;

@@ -30,6 +30,16 @@ _vp = C.c_void_p
 _lib = None
 
 
+class RequestInfo(C.Structure):
+    _fields_ = [("status", C.c_int), ("out_n", C.c_uint64), ("r_n", C.c_uint64), ("t_submit", C.c_double),
+                ("t_admit", C.c_double), ("t_done", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("in_flight_bytes", C.c_uint64), ("peak_bytes", C.c_uint64), ("waiting", C.c_uint64),
+                ("batches", C.c_uint64), ("max_concurrent_batches", C.c_uint64), ("max_batch_jobs", C.c_uint64)]
+
+
 class MulJob(C.Structure):
     """nn_mul_job: one product of a batch (device pointers)."""
     _fields_ = [("d_a", C.c_void_p), ("n_a", C.c_uint64), ("d_b", C.c_void_p), ("n_b", C.c_uint64),
@@ -88,6 +98,14 @@ def lib() -> C.CDLL:
         "nn_context_set_tunable": (C.c_int, [_vp, C.c_char_p, C.c_int64]),
         "nn_context_get_tunable": (C.c_int64, [_vp, C.c_char_p]),
         "nn_mul_base_noalloc": (C.c_int, [_vp, C.c_uint64, _vp, C.c_uint64, _vp, _vp]),
+        "nn_batch_launch": (C.c_int, [_vp, _vp, C.POINTER(MulJob)]),
+        "nn_server_create": (C.c_int, [C.c_int, C.c_uint64, C.c_int, C.c_int, C.POINTER(_vp)]),
+        "nn_server_submit_mul": (C.c_int, [_vp, _u64p, C.c_uint64, _u64p, C.c_uint64, _u64p, _u64p]),
+        "nn_server_submit_div": (C.c_int, [_vp, _u64p, C.c_uint64, _u64p, C.c_uint64, _u64p, _u64p, _u64p]),
+        "nn_server_wait": (C.c_int, [_vp, C.c_uint64, C.c_double, C.POINTER(RequestInfo)]),
+        "nn_server_get_stats": (C.c_int, [_vp, C.POINTER(ServerStats)]),
+        "nn_server_clock": (C.c_double, [_vp]),
+        "nn_server_destroy": (C.c_int, [_vp]),
         "nn_launch_count": (C.c_uint64, []),
         "nn_profile_enable": (None, [C.c_int]),
         "nn_profile_report": (C.c_uint64, [C.c_char_p, C.c_uint64]),
@@ -405,3 +423,67 @@ def profile_report() -> dict:
         name, cnt, ms = line.split()
         out[name] = (int(cnt), float(ms))
     return out
+
+
+class Server:
+    """nn_server: continuous batching of multiply/divide requests (host arrays)."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0, streams: int = 3, div_workers: int = 2):
+        h = _vp()
+        st = lib().nn_server_create(device, hbm_budget, streams, div_workers, C.byref(h))
+        if st != NN_OK:
+            raise NNError(st, "nn_server_create: " + lib().nn_status_string(st).decode())
+        self.h = h
+        self._keep = {}
+
+    def clock(self) -> float:
+        return lib().nn_server_clock(self.h)
+
+    def submit_mul(self, a, b) -> int:
+        a, b = _np(a), _np(b)
+        out = np.empty(a.size + b.size, dtype=np.uint64)
+        t = C.c_uint64()
+        st = lib().nn_server_submit_mul(self.h, _ptr(a), a.size, _ptr(b), b.size, _ptr(out), C.byref(t))
+        if st != NN_OK:
+            raise NNError(st, "submit_mul: " + lib().nn_status_string(st).decode())
+        self._keep[t.value] = ("mul", a, b, out, None)
+        return t.value
+
+    def submit_div(self, a, b) -> int:
+        a, b = _np(a), _np(b)
+        q = np.empty(a.size + 1, dtype=np.uint64)
+        r = np.empty(max(a.size, b.size) + 1, dtype=np.uint64)
+        t = C.c_uint64()
+        st = lib().nn_server_submit_div(self.h, _ptr(a), a.size, _ptr(b), b.size, _ptr(q), _ptr(r), C.byref(t))
+        if st != NN_OK:
+            raise NNError(st, "submit_div: " + lib().nn_status_string(st).decode())
+        self._keep[t.value] = ("div", a, b, q, r)
+        return t.value
+
+    def wait(self, ticket: int, timeout: float = 600.0):
+        """Returns (result, info): the product, or (quotient, remainder)."""
+        info = RequestInfo()
+        st = lib().nn_server_wait(self.h, ticket, timeout, C.byref(info))
+        kind, _, _, out, r = self._keep.pop(ticket)
+        if st != NN_OK:
+            raise NNError(st, "request failed: " + lib().nn_status_string(st).decode())
+        meta = {"submit": info.t_submit, "admit": info.t_admit, "done": info.t_done}
+        if kind == "mul":
+            return out[: info.out_n], meta
+        return (out[: info.out_n], r[: info.r_n]), meta
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        lib().nn_server_get_stats(self.h, C.byref(s))
+        return {k: getattr(s, k) for k, _ in ServerStats._fields_}
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            lib().nn_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

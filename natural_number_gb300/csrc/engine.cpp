@@ -151,13 +151,14 @@ nn_status forward(nn_context* c, nn_transform* t, const u64* d_limbs, u64 n, int
   return NN_OK;
 }
 
-nn_status inverse_save(nn_context* c, nn_transform* t, u64* d_out, u64 size, u64* written) {
+nn_status inverse_save(nn_context* c, nn_transform* t, u64* d_out, u64 size, u64* written,
+                       bool skip_last_pass = false) {
   if (size < 2) {
     c->err = "save: size must be at least 2";
     return NN_ERR_INVALID;
   }
   const std::vector<nn::Pass> plan = c->passes(t->scale);
-  NN_CK(c, nn::ntt_inverse(t->res, t->scale, c->tables, c->stream, &plan), "inverse NTT");
+  NN_CK(c, nn::ntt_inverse(t->res, t->scale, c->tables, c->stream, &plan, skip_last_pass), "inverse NTT");
   u64 w = 0;
   NN_CK(c, nn::ntt_save(t->res, t->scale, d_out, size, c->scan, &w, c->stream), "CRT/carry");
   if (written) *written = w;
@@ -175,14 +176,33 @@ nn_status pointwise(nn_context* c, nn_transform* dst, const nn_transform* a, con
   return NN_OK;
 }
 
+// The second operand's transform up to its last pass, then that pass fused
+// with the pointwise product by `other` (nullptr: square) and the first
+// inverse pass; the caller finishes with inverse_save(skip_last_pass).
+nn_status forward_fused(nn_context* c, nn_transform* t, const u64* d_limbs, u64 n, int s, const nn_transform* other) {
+  NN_CK(c, nn::tables_ensure(c->tables, s, c->stream), "twiddle tables");
+  nn_status st = xform_reserve(c, t, s);
+  if (st != NN_OK) return st;
+  const std::vector<nn::Pass> plan = c->passes(s);
+  NN_CK(c, nn::ntt_forward_head(d_limbs, n, t->res, s, c->tables, c->stream, plan), "forward NTT");
+  NN_CK(c, nn::ntt_fused_last(t->res, other ? other->res : nullptr, s, c->tables, c->stream, plan),
+        "fused pass");
+  return NN_OK;
+}
+
 // Balanced NTT product at scale s into d_out (size limbs, or wrap).
 nn_status ntt_product(nn_context* c, u64* d_out, const u64* a, u64 na, const u64* b, u64 nb, int s, u64 size,
                       u64* written) {
   nn_transform xa, xb;
   nn_status st = forward(c, &xa, a, na, s);
-  if (st == NN_OK) st = forward(c, &xb, b, nb, s);
-  if (st == NN_OK) st = pointwise(c, &xb, &xa, &xb);
-  if (st == NN_OK) st = inverse_save(c, &xb, d_out, size, written);
+  if (st == NN_OK && c->passes(s).size() >= 2) {
+    st = forward_fused(c, &xb, b, nb, s, &xa);
+    if (st == NN_OK) st = inverse_save(c, &xb, d_out, size, written, true);
+  } else {
+    if (st == NN_OK) st = forward(c, &xb, b, nb, s);
+    if (st == NN_OK) st = pointwise(c, &xb, &xa, &xb);
+    if (st == NN_OK) st = inverse_save(c, &xb, d_out, size, written);
+  }
   dev_free(c, xa.res, xa.words);
   dev_free(c, xb.res, xb.words);
   return st;
@@ -242,9 +262,15 @@ nn_status sqr_impl(nn_context* c, u64* d_out, const u64* a, u64 n) {
   // natural::_sqr_NTT (natural.h:433-442): one transform, squared pointwise.
   const int s = ntt_scale(n, n);
   nn_transform x;
-  nn_status st = forward(c, &x, a, n, s);
-  if (st == NN_OK) st = pointwise(c, &x, &x, &x);
-  if (st == NN_OK) st = inverse_save(c, &x, d_out, 2 * n, nullptr);
+  nn_status st;
+  if (c->passes(s).size() >= 2) {
+    st = forward_fused(c, &x, a, n, s, nullptr);
+    if (st == NN_OK) st = inverse_save(c, &x, d_out, 2 * n, nullptr, true);
+  } else {
+    st = forward(c, &x, a, n, s);
+    if (st == NN_OK) st = pointwise(c, &x, &x, &x);
+    if (st == NN_OK) st = inverse_save(c, &x, d_out, 2 * n, nullptr);
+  }
   dev_free(c, x.res, x.words);
   return st;
 }
@@ -313,7 +339,7 @@ nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, c
         J.lambda0[k] = plan[k].lambda0;
         J.R[k] = plan[k].R;
         J.C[k] = plan[k].C;
-        smem = std::max(smem, (size_t)plan[k].C << plan[k].R << 3);
+        smem = std::max(smem, nn::tile_smem_bytes(plan[k].C, plan[k].R));
       }
       steps[j] = 2 * J.n_pass + 2;
       B->off_a[j] = B->arena_words;
@@ -402,9 +428,7 @@ nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, c
                            cudaMemcpyHostToDevice, c->stream), "upload items");
   NN_CK(c, cudaMemcpyAsync(B->d_need, B->need.data(), B->need.size() * 4, cudaMemcpyHostToDevice, c->stream),
         "upload counts");
-  NN_CK(c, cudaHostAlloc((void**)&B->h_jobs, count * sizeof(nn::BatchJob), cudaHostAllocDefault), "pinned jobs");
   NN_CK(c, cudaEventCreateWithFlags(&B->ran, cudaEventDisableTiming), "event");
-  NN_CK(c, cudaStreamSynchronize(c->stream), "batch plan upload");
   return NN_OK;
 }
 
@@ -509,9 +533,13 @@ nn_status nn_context_create(int device, uint64_t budget, nn_context** out) {
 nn_status nn_context_destroy(nn_context* c) {
   if (!c) return NN_ERR_INVALID;
   cudaSetDevice(c->device);
-  cudaStreamSynchronize(c->stream);
+  // Work the caller ordered on its own stream must be finished (or that
+  // stream still alive); teardown itself only uses the context's stream.
+  if (c->stream != c->own) cudaStreamSynchronize(c->stream);
+  c->stream = c->own;
+  cudaStreamSynchronize(c->own);
   for (int i = 0; i < 3; ++i) dev_free(c, c->scratch[i], c->scratch_words[i]);
-  cudaStreamSynchronize(c->stream);
+  cudaStreamSynchronize(c->own);
   nn::tables_free(c->tables);
   nn::scan_free(c->scan);
   if (c->own) cudaStreamDestroy(c->own);
@@ -752,9 +780,9 @@ nn_status nn_batch_create(nn_context* c, const uint64_t* na, const uint64_t* nb,
   return NN_OK;
 }
 
-nn_status nn_batch_run(nn_context* c, nn_batch* B, const nn_mul_job* jobs) {
-  if (!c || !B || !jobs) return NN_ERR_INVALID;
-  if (B->pending) NN_CK(c, cudaEventSynchronize(B->ran), "previous batch run");
+// Fills a job table (the plan's pinned one, or `into`) for one run.
+nn_status batch_fill(nn_context* c, nn_batch* B, const nn_mul_job* jobs, nn::BatchJob* into = nullptr) {
+  nn::BatchJob* dst = into ? into : B->h_jobs;
   for (u64 j = 0; j < B->count; ++j) {
     if (jobs[j].n_a != B->na[j] || jobs[j].n_b != B->nb[j] || !jobs[j].d_a || !jobs[j].d_b || !jobs[j].d_out) {
       c->err = "batch run: job does not match the plan";
@@ -766,8 +794,43 @@ nn_status nn_batch_run(nn_context* c, nn_batch* B, const nn_mul_job* jobs) {
     J.out = jobs[j].d_out;
     J.res_a = B->d_arena + B->off_a[j];
     J.res_b = B->d_arena + B->off_b[j];
-    B->h_jobs[j] = J;
+    dst[j] = J;
   }
+  return NN_OK;
+}
+
+nn_status nn_batch_launch(nn_context* c, nn_batch* B, const nn_mul_job* jobs) {
+  if (!c || !B || !jobs) return NN_ERR_INVALID;
+  if (B->pending) NN_CK(c, cudaEventSynchronize(B->ran), "previous batch run");
+  // Pageable staging: the copy has taken the data when cudaMemcpyAsync returns,
+  // and no pinned allocation (which would synchronise the device) is needed.
+  std::vector<nn::BatchJob> table(B->count);
+  nn_status st = batch_fill(c, B, jobs, table.data());
+  if (st != NN_OK) return st;
+  NN_CK(c, cudaMemcpyAsync(B->d_jobs, table.data(), B->count * sizeof(nn::BatchJob), cudaMemcpyHostToDevice,
+                           c->stream),
+        "upload jobs");
+  NN_CK(c, cudaMemsetAsync(B->d_state, 0, (B->n_ctrs + 4) * 4, c->stream), "reset counters");
+  NN_CK(c, cudaMemsetAsync(B->d_flags, 0, (B->n_flags + 2) * 4, c->stream), "reset flags");
+  nn::launch_begin("batch_persistent", c->stream);
+  cudaError_t le = nn::batch_launch(B->d_jobs, B->d_items, (nn::u32)B->items.size(), B->d_need, B->d_state,
+                                    B->d_state + B->n_ctrs, B->d_flags, c->scan.err, c->tables, B->grid, B->smem,
+                                    c->stream);
+  nn::launch_end(c->stream);
+  NN_CK(c, le, "batch launch");
+  NN_CK(c, cudaEventRecord(B->ran, c->stream), "event record");
+  B->pending = true;
+  return NN_OK;
+}
+
+nn_status nn_batch_run(nn_context* c, nn_batch* B, const nn_mul_job* jobs) {
+  if (!c || !B || !jobs) return NN_ERR_INVALID;
+  if (B->pending) NN_CK(c, cudaEventSynchronize(B->ran), "previous batch run");
+  if (!B->h_jobs)  // pinned, so the graph's upload node can read it at replay time
+    NN_CK(c, cudaHostAlloc((void**)&B->h_jobs, B->count * sizeof(nn::BatchJob), cudaHostAllocDefault),
+          "pinned jobs");
+  nn_status fst = batch_fill(c, B, jobs);
+  if (fst != NN_OK) return fst;
   if (!B->exec) {
     nn_status st = batch_capture(c, B);
     if (st != NN_OK) return st;

@@ -37,6 +37,11 @@ struct Pass {
 // r_last: levels of the contiguous (deepest) pass; r_col: most levels of a
 // strided column pass.
 std::vector<Pass> plan_passes(int s, int r_last = 11, int r_col = 9);
+// Shared memory of a pass tile (C << R words, padded two words per 32).
+inline size_t tile_smem_bytes(int C, int R) {
+  const size_t n = (size_t)C << R;
+  return (n + n / 16 + 2) * 8;
+}
 
 // Scratch for the decoupled-lookback carry scan.
 struct Scan {
@@ -84,7 +89,15 @@ cudaError_t ntt_forward(const u64* limbs, u64 n, u64* res, int s, const Tables& 
 // Pointwise product of degree-1 residues (ntt_info.h:224-231); dst may alias a or b.
 cudaError_t ntt_pointwise(u64* dst, const u64* a, const u64* b, int s, const Tables& t, cudaStream_t st);
 // Inverse transform with the final 2^-(s-1) scale (ntt_info.h:200-221); values in [0,p).
-cudaError_t ntt_inverse(u64* res, int s, const Tables& t, cudaStream_t st, const std::vector<Pass>* plan = nullptr);
+cudaError_t ntt_inverse(u64* res, int s, const Tables& t, cudaStream_t st, const std::vector<Pass>* plan = nullptr,
+                        bool skip_last_pass = false);
+// The forward transform of limbs without its last (contiguous) pass.
+cudaError_t ntt_forward_head(const u64* limbs, u64 n, u64* res, int s, const Tables& t, cudaStream_t st,
+                             const std::vector<Pass>& plan);
+// The last forward pass of `res` fused with the pointwise product by `other`
+// (a complete forward transform; nullptr squares) and the first inverse pass.
+cudaError_t ntt_fused_last(u64* res, const u64* other, int s, const Tables& t, cudaStream_t st,
+                           const std::vector<Pass>& plan);
 // CRT + carry into `size` limbs (normal mode) or the wrapped product mod
 // B^L - 1 in L limbs when size-1 > L (ntt_info.h:237-248).  Returns the
 // number of limbs written through *written (host value).

@@ -95,10 +95,20 @@ __global__ void twiddle_extend_kernel(u64* tab, u64 n, u64 bw, u64 bwp, int prim
 // FIRST: input is limbs (n_in of them, zero beyond); otherwise residues [3][L].
 // SCALE: multiply by 2^-(s-1) on the way out (last inverse pass).
 template <int C, bool FIRST, bool INV, bool SCALE>
-__global__ void __launch_bounds__(256) ntt_pass_kernel(const u64* in, u64* out, u64 n_in, int s, int lambda0, int R,
+__global__ void __launch_bounds__(256, 4) ntt_pass_kernel(const u64* in, u64* out, u64 n_in, int s, int lambda0, int R,
                                                        const u64* __restrict__ tab, u64 tab_stride) {
   extern __shared__ u64 sm[];
   pass_tile<C, FIRST, INV, SCALE, false>(sm, in, out, n_in, s, lambda0, R, tab, tab_stride, blockIdx.y, blockIdx.x);
+}
+
+// Contiguous last pass: forward levels, pointwise by `other` (nullptr
+// squares), inverse levels, in one visit of each tile.
+__global__ void __launch_bounds__(256, 3) ntt_fused_kernel(u64* res, const u64* other, int s, int lambda0, int R,
+                                                        const u64* __restrict__ tab, const u64* __restrict__ itab,
+                                                        u64 tab_stride) {
+  extern __shared__ u64 sm[];
+  pass_tile<2, false, false, false, false, true>(sm, res, res, 0, s, lambda0, R, tab, tab_stride, blockIdx.y,
+                                                 blockIdx.x, itab, other);
 }
 
 __global__ void __launch_bounds__(256) pointwise_kernel(u64* dst, const u64* a, const u64* b, u64 L,
@@ -110,7 +120,7 @@ __global__ void __launch_bounds__(256) pointwise_kernel(u64* dst, const u64* a, 
 
 template <int C, bool FIRST, bool INV, bool SCALE>
 cudaError_t launch_pass(const u64* in, u64* out, u64 n_in, int s, const Pass& ps, const Tables& t, cudaStream_t st) {
-  const size_t smem = (size_t)ps.C << ps.R << 3;
+  const size_t smem = tile_smem_bytes(ps.C, ps.R);
   static bool configured = false;
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(ntt_pass_kernel<C, FIRST, INV, SCALE>,
@@ -242,9 +252,40 @@ cudaError_t ntt_forward(const u64* limbs, u64 n, u64* res, int s, const Tables& 
   return cudaSuccess;
 }
 
-cudaError_t ntt_inverse(u64* res, int s, const Tables& t, cudaStream_t st, const std::vector<Pass>* given) {
+cudaError_t ntt_forward_head(const u64* limbs, u64 n, u64* res, int s, const Tables& t, cudaStream_t st,
+                             const std::vector<Pass>& plan) {
+  if (plan.size() < 2) return cudaErrorInvalidValue;  // the fused pass would have to load limbs
+  for (size_t k = 0; k + 1 < plan.size(); ++k) {
+    cudaError_t e = k == 0 ? dispatch_pass<true, false, false>(limbs, res, n, s, plan[k], t, st)
+                           : dispatch_pass<false, false, false>(res, res, 0, s, plan[k], t, st);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t ntt_fused_last(u64* res, const u64* other, int s, const Tables& t, cudaStream_t st,
+                           const std::vector<Pass>& plan) {
+  const Pass& ps = plan.back();
+  if (ps.C != 2) return cudaErrorInvalidValue;
+  const size_t smem = tile_smem_bytes(ps.C, ps.R);
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(ntt_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  const u64 tiles = (1ull << s) / ((u64)ps.C << ps.R);
+  dim3 grid((unsigned)tiles, 3);
+  launch_begin("ntt_fused_row_pass", st);
+  ntt_fused_kernel<<<grid, 256, smem, st>>>(res, other, s, ps.lambda0, ps.R, t.root, t.iroot, t.cap);
+  launch_end(st);
+  return cudaGetLastError();
+}
+
+cudaError_t ntt_inverse(u64* res, int s, const Tables& t, cudaStream_t st, const std::vector<Pass>* given,
+                        bool skip_last_pass) {
   std::vector<Pass> plan = given ? *given : plan_passes(s);
-  for (size_t k = plan.size(); k-- > 0;) {
+  for (size_t k = plan.size() - (skip_last_pass ? 1 : 0); k-- > 0;) {
     cudaError_t e = k == 0 ? dispatch_pass<false, true, true>(res, res, 0, s, plan[k], t, st)
                            : dispatch_pass<false, true, false>(res, res, 0, s, plan[k], t, st);
     if (e != cudaSuccess) return e;

@@ -1,15 +1,47 @@
 // ntt_tiles.cuh — tile-level device code of the NTT passes and the pointwise
 // product, shared by the per-call kernels (ntt.cu) and the persistent batch
 // kernel (batch.cu).  See ntt.cu for the level/pass decomposition.
+//
+// Every routine is specialised per prime (template PR), so the modulus and
+// its reduction constants are immediates.  In-tile indices are 32-bit.  The
+// shared-memory tile is padded by two words per 32 words, which spreads the
+// strided accesses of the deepest levels over the banks.
 #pragma once
 
 #include "nn_device.cuh"
 
 namespace nn {
 
-// Residue loads/stores.  The persistent kernel reads data other CTAs wrote
-// earlier in the same launch, so it bypasses L1 (.cg); per-call kernels use
-// plain accesses.
+// Compile-time constants of p_i = c_i * 2^56 + 1 (ntt_info.h:69-73).
+template <int PR>
+struct PrimeC {
+  static constexpr u64 c = PR == 0 ? 27 : PR == 1 ? 58 : 87;
+  static constexpr u64 p = c << 56 | 1;
+  static constexpr u32 c_hi = (u32)(c << 24);
+  static constexpr u64 m64 = PR == 0 ? 10 : PR == 1 ? 5 : 3;  // ceil(2^64 / p)
+  // floor(2^(124+i) / p_i): the reference's Barrett constants (asmLinux.asm:926, 1075, 1236)
+  static constexpr u64 mu = PR == 0 ? 0x97b425ed097b4259ull : PR == 1 ? 0x8d3dcb08d3dcb08aull : 0xbc52640bc52640baull;
+};
+
+// Exact reduction of T < 2p^2 with the reference's Barrett constant and two
+// conditional subtractions (see barrett() in nn_device.cuh).
+template <int PR>
+__device__ __forceinline__ u64 barrett_c(U128 t) {
+  constexpr u64 p = PrimeC<PR>::p;
+  constexpr int sh = 60 + PR;
+  const u64 top = (t.hi << (64 - sh)) | (t.lo >> sh);
+  const u64 q = mulhi(top, PrimeC<PR>::mu);
+  u64 r = t.lo - mul_p(q, PrimeC<PR>::c_hi);
+  if (r >= p) r -= p;
+  if (r >= p) r -= p;
+  return r;
+}
+
+// Shared-memory padding: two words per 32, so pairs of words stay 16-byte
+// aligned (16-byte async copies) while strided accesses of the deep levels
+// spread over the banks.
+__device__ __forceinline__ u32 pad16(u32 x) { return x + ((x >> 5) << 1); }
+
 template <bool CG>
 __device__ __forceinline__ ulonglong2 ld2(const u64* p) {
   const ulonglong2* q = reinterpret_cast<const ulonglong2*>(p);
@@ -25,29 +57,32 @@ __device__ __forceinline__ void st2(u64* p, ulonglong2 v) {
     *q = v;
 }
 
-template <int K, int C, bool INV>
-__device__ __forceinline__ void level_group(u64* sm, int l, int R, u64 ksb, const u64* __restrict__ tw, u64 p,
-                                            u32 ch) {
+// K levels [l, l+K) of a tile held in shared memory: each thread takes units
+// of 2^K rows of one column and runs the radix-2^K network in registers.
+template <int K, int C, bool INV, int PR>
+__device__ __forceinline__ void level_group(u64* sm, int l, int R, u64 ksb, const u64* __restrict__ tw) {
+  constexpr u64 p = PrimeC<PR>::p;
+  constexpr u32 ch = PrimeC<PR>::c_hi;
   const int nsub = R - l - K;
-  const int units = C << (R - K);
-  for (int u = threadIdx.x; u < units; u += blockDim.x) {
-    const int i = u & (C - 1);
-    const int v = u / C;
-    const int t0 = v & ((1 << nsub) - 1);
-    const int rb = v >> nsub;
-    const int row0 = (rb << (R - l)) + t0;
-    const int rstep = 1 << nsub;
-    const u64 bidx = (ksb << l) + (u64)rb;
+  const u32 units = (u32)C << (R - K);
+  const u32 tmask = (1u << nsub) - 1;
+  const ulonglong2* twv = reinterpret_cast<const ulonglong2*>(tw);
+  for (u32 u = threadIdx.x; u < units; u += blockDim.x) {
+    const u32 i = u & (C - 1);
+    const u32 v = u / C;
+    const u32 rb = v >> nsub;
+    const u32 row0 = (rb << (R - l)) + (v & tmask);
+    const u64 bidx = (ksb << l) + rb;
     u64 x[1 << K];
 #pragma unroll
-    for (int m = 0; m < (1 << K); ++m) x[m] = sm[(row0 + m * rstep) * C + i];
+    for (int m = 0; m < (1 << K); ++m) x[m] = sm[pad16(((row0 + ((u32)m << nsub)) * C) + i)];
     if (!INV) {
 #pragma unroll
       for (int lv = 0; lv < K; ++lv) {
         const int half = (1 << K) >> (lv + 1);
 #pragma unroll
         for (int g = 0; g < (1 << lv); ++g) {
-          const ulonglong2 wv = __ldg(reinterpret_cast<const ulonglong2*>(tw) + ((bidx << lv) + g));
+          const ulonglong2 wv = __ldg(twv + ((bidx << lv) + g));
 #pragma unroll
           for (int m = 0; m < half; ++m) fwd_bfly(x[g * 2 * half + m], x[g * 2 * half + m + half], wv.x, wv.y, p, ch);
         }
@@ -58,80 +93,162 @@ __device__ __forceinline__ void level_group(u64* sm, int l, int R, u64 ksb, cons
         const int half = (1 << K) >> (lv + 1);
 #pragma unroll
         for (int g = 0; g < (1 << lv); ++g) {
-          const ulonglong2 wv = __ldg(reinterpret_cast<const ulonglong2*>(tw) + ((bidx << lv) + g));
+          const ulonglong2 wv = __ldg(twv + ((bidx << lv) + g));
 #pragma unroll
           for (int m = 0; m < half; ++m) inv_bfly(x[g * 2 * half + m], x[g * 2 * half + m + half], wv.x, wv.y, p, ch);
         }
       }
     }
 #pragma unroll
-    for (int m = 0; m < (1 << K); ++m) sm[(row0 + m * rstep) * C + i] = x[m];
+    for (int m = 0; m < (1 << K); ++m) sm[pad16(((row0 + ((u32)m << nsub)) * C) + i)] = x[m];
   }
 }
 
+// Levels per register group: as even as possible, at most kMaxGroupLevels, and at most what
+// keeps every thread of the CTA busy (units = C * 2^(R-K) >= blockDim).
+// Radix-8 at most: radix-16 units need ~100 registers and halve occupancy,
+// which costs more than the saved shared-memory round trips.
+constexpr int kMaxGroupLevels = 3;
+
+__device__ __forceinline__ int group_cap(int C, int R) {
+  int k = R < kMaxGroupLevels ? R : kMaxGroupLevels;
+  while (k > 1 && ((u32)C << (R - k)) < blockDim.x) --k;
+  return k;
+}
+
+template <int C, bool INV, int PR>
+__device__ __forceinline__ void run_group(u64* sm, int k, int l, int R, u64 ksb, const u64* tw) {
+  if (k == 3)
+    level_group<3, C, INV, PR>(sm, l, R, ksb, tw);
+  else if (k == 2)
+    level_group<2, C, INV, PR>(sm, l, R, ksb, tw);
+  else
+    level_group<1, C, INV, PR>(sm, l, R, ksb, tw);
+}
+
+// Forward levels [0, R) of the tile in shared memory.
+template <int C, int PR>
+__device__ __forceinline__ void tile_forward(u64* sm, int R, u64 ksb, const u64* tw) {
+  const int cap = group_cap(C, R);
+  const int n = (R + cap - 1) / cap;
+  for (int g = 0, l = 0; g < n; ++g) {
+    const int k = (R - l + (n - g) - 1) / (n - g);
+    run_group<C, false, PR>(sm, k, l, R, ksb, tw);
+    __syncthreads();
+    l += k;
+  }
+}
+
+// Inverse levels R-1 .. 0 of the tile in shared memory.
+template <int C, int PR>
+__device__ __forceinline__ void tile_inverse(u64* sm, int R, u64 ksb, const u64* tw) {
+  const int cap = group_cap(C, R);
+  const int n = (R + cap - 1) / cap;
+  for (int g = 0, l = R; g < n; ++g) {
+    const int k = (l + (n - g) - 1) / (n - g);
+    l -= k;
+    run_group<C, true, PR>(sm, k, l, R, ksb, tw);
+    __syncthreads();
+  }
+}
+
+// Pointwise product of one group of 4 residues (a0..a3)(b0..b3), raw [0,2p)
+// inputs, [0,p) outputs: degree-1 residues mod (x^2 - w) and (x^2 + w),
+// w = root[2g] (ntt_info.h:224-231, asmLinux.asm:910-1057).
+template <int PR>
+__device__ __forceinline__ void pointwise4(u64 (&o)[4], const u64 (&A)[4], const u64 (&Bv)[4], ulonglong2 wv) {
+  constexpr u64 p = PrimeC<PR>::p;
+  constexpr u32 ch = PrimeC<PR>::c_hi;
+  const u64 a0 = reduce2p(A[0], p), a1 = reduce2p(A[1], p), a2 = reduce2p(A[2], p), a3 = reduce2p(A[3], p);
+  const u64 b0 = reduce2p(Bv[0], p), b1 = reduce2p(Bv[1], p), b2 = reduce2p(Bv[2], p), b3 = reduce2p(Bv[3], p);
+  const u64 wb1 = shoup_mul(b1, wv.x, wv.y, p, ch);
+  const u64 wb3 = shoup_mul(b3, wv.x, wv.y, p, ch);
+  const u64 nwb3 = wb3 ? p - wb3 : 0;
+  o[0] = barrett_c<PR>(add128(mul_wide(a0, b0), mul_wide(a1, wb1)));
+  o[1] = barrett_c<PR>(add128(mul_wide(a0, b1), mul_wide(a1, b0)));
+  o[2] = barrett_c<PR>(add128(mul_wide(a2, b2), mul_wide(a3, nwb3)));
+  o[3] = barrett_c<PR>(add128(mul_wide(a2, b3), mul_wide(a3, b2)));
+}
+
 // One tile of a pass over levels [lambda0, lambda0+R): C columns x 2^R rows of
-// one prime.  FIRST: `in` is n_in limbs (zero beyond) reduced on the fly;
+// prime PR.  FIRST: `in` is n_in limbs (zero beyond) reduced on the fly;
 // otherwise residues [3][2^s].  SCALE: multiply by 2^-(s-1) on the way out.
-template <int C, bool FIRST, bool INV, bool SCALE, bool CG>
-__device__ __forceinline__ void pass_tile(u64* sm, const u64* in, u64* out, u64 n_in, int s, int lambda0, int R,
-                                          const u64* __restrict__ tab, u64 tab_stride, int prime, u64 tile) {
-  const u64 p = g_primes.p[prime];
-  const u32 ch = g_primes.c_hi[prime];
+// FUSED (contiguous passes only): after the forward levels, multiply
+// pointwise by the other operand's residues `other` and run the inverse
+// levels before writing back.
+template <int C, bool FIRST, bool INV, bool SCALE, bool CG, bool FUSED, int PR>
+__device__ __forceinline__ void pass_tile_p(u64* sm, const u64* in, u64* out, u64 n_in, int s, int lambda0, int R,
+                                            const u64* __restrict__ tab, const u64* __restrict__ itab, u64 tab_stride,
+                                            u64 tile, const u64* other) {
+  constexpr u64 p = PrimeC<PR>::p;
+  constexpr u32 ch = PrimeC<PR>::c_hi;
   const u64 L = 1ull << s;
-  const u64* tw = tab + (u64)prime * tab_stride;
+  const u64* tw = tab + (u64)PR * tab_stride;
   const int lg_s = s - lambda0 - R;
   const u64 tiles_per_sb = (1ull << lg_s) / C;
   const u64 ksb = tile / tiles_per_sb;
   const u64 base = (ksb << (lg_s + R)) + (tile % tiles_per_sb) * C;
-  const int nel = C << R;
+  const u32 nel = (u32)C << R;
+  constexpr int LGC = C == 16 ? 4 : 1;
 
   if (FIRST) {
-    const u64 m64 = g_primes.m64[prime];
-    for (int idx = threadIdx.x; idx < nel; idx += blockDim.x) {
-      const u64 pos = base + ((u64)(idx / C) << lg_s) + (idx & (C - 1));
-      sm[idx] = pos < n_in ? limb_mod(in[pos], m64, p, ch) : 0;
+    const bool vec = ((reinterpret_cast<unsigned long long>(in) & 15) == 0);
+    for (u32 idx = 2 * threadIdx.x; idx < nel; idx += 2 * blockDim.x) {
+      const u64 pos = base + ((u64)(idx >> LGC) << lg_s) + (idx & (C - 1));
+      u64 x0 = 0, x1 = 0;
+      if (vec && pos + 1 < n_in) {
+        const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(in + pos);
+        x0 = v.x;
+        x1 = v.y;
+      } else {
+        if (pos < n_in) x0 = in[pos];
+        if (pos + 1 < n_in) x1 = in[pos + 1];
+      }
+      sm[pad16(idx)] = pos < n_in ? limb_mod(x0, PrimeC<PR>::m64, p, ch) : 0;
+      sm[pad16(idx + 1)] = pos + 1 < n_in ? limb_mod(x1, PrimeC<PR>::m64, p, ch) : 0;
     }
   } else {
-    const u64* src = in + (u64)prime * L;
-    for (int idx = 2 * threadIdx.x; idx < nel; idx += 2 * blockDim.x) {
-      const u64 pos = base + ((u64)(idx / C) << lg_s) + (idx & (C - 1));
+    const u64* src = in + (u64)PR * L;
+    for (u32 idx = 2 * threadIdx.x; idx < nel; idx += 2 * blockDim.x) {
+      const u64 pos = base + ((u64)(idx >> LGC) << lg_s) + (idx & (C - 1));
       const ulonglong2 v = ld2<CG>(src + pos);
-      sm[idx] = v.x;
-      sm[idx + 1] = v.y;
+      sm[pad16(idx)] = v.x;
+      sm[pad16(idx + 1)] = v.y;
     }
   }
   __syncthreads();
 
   if (!INV) {
-    for (int l = 0; l < R;) {
-      const int k = R - l >= 3 ? 3 : R - l;
-      if (k == 3)
-        level_group<3, C, false>(sm, l, R, ksb, tw, p, ch);
-      else if (k == 2)
-        level_group<2, C, false>(sm, l, R, ksb, tw, p, ch);
-      else
-        level_group<1, C, false>(sm, l, R, ksb, tw, p, ch);
+    tile_forward<C, PR>(sm, R, ksb, tw);
+    if (FUSED) {  // contiguous tile: smem index == position - base; other == nullptr squares
+      const u64* oth = other ? other + (u64)PR * L : nullptr;
+      const ulonglong2* twv = reinterpret_cast<const ulonglong2*>(tw);
+      for (u32 g4 = 4 * threadIdx.x; g4 < nel; g4 += 4 * blockDim.x) {
+        const u64 Bv[4] = {sm[pad16(g4)], sm[pad16(g4 + 1)], sm[pad16(g4 + 2)], sm[pad16(g4 + 3)]};
+        u64 A[4] = {Bv[0], Bv[1], Bv[2], Bv[3]};
+        if (oth) {
+          const ulonglong2 A0 = ld2<CG>(oth + base + g4), A1 = ld2<CG>(oth + base + g4 + 2);
+          A[0] = A0.x;
+          A[1] = A0.y;
+          A[2] = A1.x;
+          A[3] = A1.y;
+        }
+        u64 o[4];
+        pointwise4<PR>(o, A, Bv, __ldg(twv + ((base + g4) >> 2)));
+#pragma unroll
+        for (int q = 0; q < 4; ++q) sm[pad16(g4 + q)] = o[q];
+      }
       __syncthreads();
-      l += k;
+      tile_inverse<C, PR>(sm, R, ksb, itab + (u64)PR * tab_stride);
     }
   } else {
-    for (int l = R; l > 0;) {
-      const int k = l >= 3 ? 3 : l;
-      l -= k;
-      if (k == 3)
-        level_group<3, C, true>(sm, l, R, ksb, tw, p, ch);
-      else if (k == 2)
-        level_group<2, C, true>(sm, l, R, ksb, tw, p, ch);
-      else
-        level_group<1, C, true>(sm, l, R, ksb, tw, p, ch);
-      __syncthreads();
-    }
+    tile_inverse<C, PR>(sm, R, ksb, tw);
   }
 
-  u64* dst = out + (u64)prime * L;
-  for (int idx = 2 * threadIdx.x; idx < nel; idx += 2 * blockDim.x) {
-    const u64 pos = base + ((u64)(idx / C) << lg_s) + (idx & (C - 1));
-    ulonglong2 v = make_ulonglong2(sm[idx], sm[idx + 1]);
+  u64* dst = out + (u64)PR * L;
+  for (u32 idx = 2 * threadIdx.x; idx < nel; idx += 2 * blockDim.x) {
+    const u64 pos = base + ((u64)(idx >> LGC) << lg_s) + (idx & (C - 1));
+    ulonglong2 v = make_ulonglong2(sm[pad16(idx)], sm[pad16(idx + 1)]);
     if (SCALE) {
       v.x = div_pow2(v.x, (u32)(s - 1), p);
       v.y = div_pow2(v.y, (u32)(s - 1), p);
@@ -140,30 +257,39 @@ __device__ __forceinline__ void pass_tile(u64* sm, const u64* in, u64* out, u64 
   }
 }
 
-// Pointwise product of one group g (4 residues) of prime i: degree-1 residues
-// mod (x^2 - w) and (x^2 + w), w = root[2g] (ntt_info.h:224-231,
-// asmLinux.asm:910-1057).  Inputs in [0,2p), outputs in [0,p).
+template <int C, bool FIRST, bool INV, bool SCALE, bool CG, bool FUSED = false>
+__device__ __forceinline__ void pass_tile(u64* sm, const u64* in, u64* out, u64 n_in, int s, int lambda0, int R,
+                                          const u64* __restrict__ tab, u64 tab_stride, int prime, u64 tile,
+                                          const u64* __restrict__ itab = nullptr, const u64* other = nullptr) {
+  if (prime == 0)
+    pass_tile_p<C, FIRST, INV, SCALE, CG, FUSED, 0>(sm, in, out, n_in, s, lambda0, R, tab, itab, tab_stride, tile,
+                                                   other);
+  else if (prime == 1)
+    pass_tile_p<C, FIRST, INV, SCALE, CG, FUSED, 1>(sm, in, out, n_in, s, lambda0, R, tab, itab, tab_stride, tile,
+                                                   other);
+  else
+    pass_tile_p<C, FIRST, INV, SCALE, CG, FUSED, 2>(sm, in, out, n_in, s, lambda0, R, tab, itab, tab_stride, tile,
+                                                   other);
+}
+
+// Pointwise product of one group g (4 residues) of prime i.
 template <bool CG>
 __device__ __forceinline__ void pointwise_group(u64* dst, const u64* a, const u64* b, u64 L,
                                                 const u64* __restrict__ tab, u64 tab_stride, int i, u64 g) {
-  const u64 p = g_primes.p[i];
-  const u32 ch = g_primes.c_hi[i];
   const ulonglong2 wv = __ldg(reinterpret_cast<const ulonglong2*>(tab + (u64)i * tab_stride) + g);
   const u64 off = (u64)i * L + 4 * g;
   const ulonglong2 A0 = ld2<CG>(a + off), A1 = ld2<CG>(a + off + 2);
   const ulonglong2 B0 = ld2<CG>(b + off), B1 = ld2<CG>(b + off + 2);
-  const u64 a0 = reduce2p(A0.x, p), a1 = reduce2p(A0.y, p), a2 = reduce2p(A1.x, p), a3 = reduce2p(A1.y, p);
-  const u64 b0 = reduce2p(B0.x, p), b1 = reduce2p(B0.y, p), b2 = reduce2p(B1.x, p), b3 = reduce2p(B1.y, p);
-  const u64 wb1 = shoup_mul(b1, wv.x, wv.y, p, ch);
-  const u64 wb3 = shoup_mul(b3, wv.x, wv.y, p, ch);
-  const u64 nwb3 = wb3 ? p - wb3 : 0;
-  ulonglong2 R0, R1;
-  R0.x = barrett(add128(mul_wide(a0, b0), mul_wide(a1, wb1)), i);
-  R0.y = barrett(add128(mul_wide(a0, b1), mul_wide(a1, b0)), i);
-  R1.x = barrett(add128(mul_wide(a2, b2), mul_wide(a3, nwb3)), i);
-  R1.y = barrett(add128(mul_wide(a2, b3), mul_wide(a3, b2)), i);
-  st2<CG>(dst + off, R0);
-  st2<CG>(dst + off + 2, R1);
+  const u64 A[4] = {A0.x, A0.y, A1.x, A1.y}, Bv[4] = {B0.x, B0.y, B1.x, B1.y};
+  u64 o[4];
+  if (i == 0)
+    pointwise4<0>(o, A, Bv, wv);
+  else if (i == 1)
+    pointwise4<1>(o, A, Bv, wv);
+  else
+    pointwise4<2>(o, A, Bv, wv);
+  st2<CG>(dst + off, make_ulonglong2(o[0], o[1]));
+  st2<CG>(dst + off + 2, make_ulonglong2(o[2], o[3]));
 }
 
 }  // namespace nn

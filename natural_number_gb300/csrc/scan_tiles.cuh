@@ -23,9 +23,9 @@ struct CrtProducerT {
   const u64* res;
   u64 L;
   u64 count;
+  static constexpr bool kBulk = true;
   __device__ __forceinline__ W3 operator()(u64 k) const {
     if (k >= count) return W3{0, 0, 0};
-    const PrimeSet& P = g_primes;
     u64 x0, x1, x2;
     if (CG) {
       x0 = __ldcg(res + k);
@@ -36,6 +36,30 @@ struct CrtProducerT {
       x1 = res[L + k];
       x2 = res[2 * L + k];
     }
+    return garner(x0, x1, x2);
+  }
+  // Eight consecutive positions from k0 (a multiple of 8) with 16-byte loads.
+  __device__ __forceinline__ void bulk(u64 k0, W3 (&x)[kScanE]) const {
+    if (k0 + kScanE > count) {
+#pragma unroll
+      for (int e = 0; e < kScanE; ++e) x[e] = (*this)(k0 + e);
+      return;
+    }
+    u64 r[3][kScanE];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int e = 0; e < kScanE; e += 2) {
+        const ulonglong2* q = reinterpret_cast<const ulonglong2*>(res + (u64)i * L + k0 + e);
+        const ulonglong2 v = CG ? __ldcg(q) : *q;
+        r[i][e] = v.x;
+        r[i][e + 1] = v.y;
+      }
+#pragma unroll
+    for (int e = 0; e < kScanE; ++e) x[e] = garner(r[0][e], r[1][e], r[2][e]);
+  }
+  __device__ __forceinline__ W3 garner(u64 x0, u64 x1, u64 x2) const {
+    const PrimeSet& P = g_primes;
     const u64 p1 = P.p[1], p2 = P.p[2];
     const u64 d1 = x1 >= x0 ? x1 - x0 : x1 + p1 - x0;
     const u64 u = shoup_mul(d1, P.inv01, P.inv01s, p1, P.c_hi[1]);
@@ -69,6 +93,8 @@ typedef CrtProducerT<false> CrtProducer;
 
 // Column sums of a schoolbook product (asmMul1's column order, asmLinux.asm:188-278).
 struct ColumnProducer {
+  static constexpr bool kBulk = false;
+  __device__ __forceinline__ void bulk(u64, W3 (&)[kScanE]) const {}
   const u64* a;
   u64 na;
   const u64* b;
@@ -94,6 +120,8 @@ struct ColumnProducer {
 
 // x[k] + y[k - shift] (two words).
 struct AddProducer {
+  static constexpr bool kBulk = false;
+  __device__ __forceinline__ void bulk(u64, W3 (&)[kScanE]) const {}
   const u64* x;
   u64 nx;
   const u64* y;
@@ -131,10 +159,16 @@ __device__ __forceinline__ void scan_tile(const Prod& prod, u64 tile, u64 total,
 
   u64 y[E];
   u64 c0 = 0, c1 = 0;
+  W3 xs[E];
+  if (Prod::kBulk && k0 + E <= total) {
+    prod.bulk(k0, xs);
+  } else {
+#pragma unroll
+    for (int e = 0; e < E; ++e) xs[e] = k0 + e < total ? prod(k0 + e) : W3{0, 0, 0};
+  }
 #pragma unroll
   for (int e = 0; e < E; ++e) {
-    const u64 k = k0 + e;
-    W3 x = k < total ? prod(k) : W3{0, 0, 0};
+    const W3 x = xs[e];
     const u64 s0 = x.w0 + c0;
     const u64 cy0 = s0 < c0;
     u64 s1 = x.w1 + c1;

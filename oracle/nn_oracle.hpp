@@ -33,6 +33,14 @@ using u128 = unsigned __int128;
 
 static inline u64 hi64(u128 x) { return (u64)(x >> 64); }
 
+// Thrown where the reference's Newton division would break one of its own
+// size preconditions (it then reads or copies out of bounds).
+struct PreconditionBroken {};
+inline unsigned long long& fallback_count() {
+  static unsigned long long n = 0;
+  return n;
+}
+
 // ---------------------------------------------------------------------------
 // Limb primitives (asm.h:7-61; asmLinux.asm:7-344, 720-751)
 // ---------------------------------------------------------------------------
@@ -1014,8 +1022,10 @@ inline Nat reciprocal2(const Nat& divs, u64 divd_size) {
     if (nxt_acc == kNttDivThreshold) nxt_acc = kNttDivThreshold - 1;
     shr_inplace(tmp, (2 * cur_acc - nxt_acc) << 6);
     if (tmp.is_zero()) tmp = Nat(1);
+    if (nxt_acc < cur_acc) throw PreconditionBroken();  // natural.h:614 would shift by a negative count
     mul_load(tmp, ans, tmp, xans);
     ans = shl(ans, (nxt_acc - cur_acc) << 6);
+    if (tmp.n < cur_acc || tmp.n - cur_acc > ans.n) throw PreconditionBroken();  // natural.h:615 add() needs it
     add(ans.data(), ans.data(), ans.n, tmp.data() + cur_acc, tmp.n - cur_acc);
   }
 }
@@ -1066,7 +1076,9 @@ inline Nat reciprocal3(const Nat& divisor, u64 dividend_size, Xform& xdiv) {
     }
     mul_load(tmp, ans, tmp, xans);
     shr_inplace(tmp, prev_acc << 6);
+    if (cur_acc < prev_acc) throw PreconditionBroken();  // natural.h:670-672 would memset a negative length
     u64 inc_acc = cur_acc - prev_acc;
+    if (inc_acc < tmp.n && tmp.n - inc_acc > prev_acc) throw PreconditionBroken();  // natural.h:676 add() needs it
     tmp.reserve(cur_acc);
     if (inc_acc >= tmp.n) {
       std::memset(tmp.data() + tmp.n, 0, sizeof(u64) * (inc_acc - tmp.n));
@@ -1115,6 +1127,7 @@ inline void div_iterative(const Nat& divd, const Nat& divs, Nat& q, Nat& r) {
     shr_inplace(tmp, rec.n << 6);
     add(q.data() + idx, q.data() + idx, q.n - idx, tmp.data(), tmp.n);
     mul_load(tmp, b, tmp, xb);
+    if (r.n < idx || r.n - idx < tmp.n) throw PreconditionBroken();  // natural.h:724 sub() needs it
     sub(r.data() + idx, r.data() + idx, r.n - idx, tmp.data(), tmp.n);
     r.norm();
     if (xb.scale) {
@@ -1128,11 +1141,65 @@ inline void div_iterative(const Nat& divd, const Nat& divs, Nat& q, Nat& r) {
     }
     if (idx == 0) break;
   }
-  while (r >= b) {
+  for (int guard = 0; r >= b; ++guard) {
+    if (guard > 64) throw PreconditionBroken();  // the block estimates were meant to be within a few units
     q = addn(q, Nat(1));
     r = subn(r, b);
   }
   shr_inplace(r, n_shl);
+}
+
+// Knuth's algorithm D (TAOCP vol. 2, 4.3.1): exact long division, used where
+// the reference's Newton division breaks its own preconditions (on such
+// inputs the reference itself reads or copies out of bounds and aborts).
+inline void div_knuth(const Nat& a, const Nat& b, Nat& q, Nat& r) {
+  const u64 n = b.n, m = a.n - b.n;
+  const unsigned sh = (unsigned)std::countl_zero(b[n - 1]);
+  std::vector<u64> v(n), u(a.n + 1);
+  for (u64 i = n; i-- > 0;) v[i] = (b[i] << sh) | (sh && i ? b[i - 1] >> (64 - sh) : 0);
+  u[a.n] = sh ? a[a.n - 1] >> (64 - sh) : 0;
+  for (u64 i = a.n; i-- > 0;) u[i] = (a[i] << sh) | (sh && i ? a[i - 1] >> (64 - sh) : 0);
+  q.resize(m + 1);
+  for (u64 j = m + 1; j-- > 0;) {
+    u128 num = ((u128)u[j + n] << 64) | u[j + n - 1];
+    u128 qh = num / v[n - 1], rh = num % v[n - 1];
+    while (qh >> 64 || (n > 1 && qh * v[n - 2] > ((rh << 64) | u[j + n - 2]))) {
+      --qh;
+      rh += v[n - 1];
+      if (rh >> 64) break;
+    }
+    u64 borrow = 0, carry = 0;
+    for (u64 i = 0; i < n; ++i) {
+      u128 p = (u128)(u64)qh * v[i] + carry;
+      carry = hi64(p);
+      u64 t = u[i + j] - (u64)p;
+      u64 b1 = u[i + j] < (u64)p;
+      u64 t2 = t - borrow;
+      u64 b2 = t < borrow;
+      u[i + j] = t2;
+      borrow = b1 | b2;
+    }
+    u64 t = u[j + n] - carry;
+    u64 b1 = u[j + n] < carry;
+    u64 t2 = t - borrow;
+    u64 b2 = t < borrow;
+    u[j + n] = t2;
+    if (b1 | b2) {  // added back: the estimate was one too large
+      --qh;
+      u64 c = 0;
+      for (u64 i = 0; i < n; ++i) {
+        u128 s2 = (u128)u[i + j] + v[i] + c;
+        u[i + j] = (u64)s2;
+        c = hi64(s2);
+      }
+      u[j + n] += c;
+    }
+    q[j] = (u64)qh;
+  }
+  q.norm();
+  r.resize(n);
+  for (u64 i = 0; i < n; ++i) r[i] = (u[i] >> sh) | (sh && i + 1 < n + 1 ? (u[i + 1] << (64 - sh)) : 0);
+  r.norm();
 }
 
 // natural.h:749-769 — returns the quotient, writes the remainder.
@@ -1151,7 +1218,12 @@ inline Nat divmod(const Nat& a, const Nat& b, Nat& r) {
     r = Nat(div_base(a, b[0], q));
     return q;
   }
-  div_iterative(a, b, q, r);
+  try {
+    div_iterative(a, b, q, r);
+  } catch (const PreconditionBroken&) {
+    ++fallback_count();
+    div_knuth(a, b, q, r);
+  }
   return q;
 }
 

@@ -57,6 +57,8 @@ extern "C" {
 
 void nno_free(void* p) { std::free(p); }
 
+unsigned long long nno_div_fallbacks(void) { return nno::fallback_count(); }
+
 u64* nno_mul(const u64* a, u64 na, const u64* b, u64 nb, u64* out_n) {
   return export_limbs(nno::mul(make(a, na), make(b, nb)), out_n);
 }

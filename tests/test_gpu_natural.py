@@ -97,3 +97,30 @@ def test_cpp_dropin_program(golden, tmp_path):
     assert int(out[1], 16) == A // B and int(out[2]) == A % B
     import math
     assert int(out[4]) == math.factorial(2000)
+
+
+# Divisions on which the reference's own Newton division aborts
+# (natural.h:670-676); the product takes its exact Newton division instead.
+REFERENCE_ABORTS = [(5046, 7406, 5047, 3703), (19141, 4406, 19142, 2203)]
+
+
+def test_divisions_the_reference_cannot_do(ctx):
+    from oracle import to_int
+    for sa, na, sb, nb in REFERENCE_ABORTS:
+        a, b = limbs(sa, na), limbs(sb, nb)
+        q, r = ctx.div(a, b)
+        A, B = to_int(a), to_int(b)
+        assert to_int(q) == A // B and to_int(r) == A % B
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_random_2n_by_n_divisions(ctx, seed):
+    """Random 2n-by-n divisions (the served division shape) against Python integers."""
+    from oracle import to_int
+    from natural_number_gb300.synth import log_uniform_sizes
+    for k, n in enumerate(log_uniform_sizes(100 + seed, 40, 1, 13)):
+        n = max(2, int(n))
+        a, b = limbs(seed * 10000 + 2 * k, 2 * n), limbs(seed * 10000 + 2 * k + 1, n)
+        q, r = ctx.div(a, b)
+        A, B = to_int(a), to_int(b)
+        assert to_int(q) == A // B and to_int(r) == A % B, n

@@ -115,3 +115,19 @@ def test_oracle_against_python_int(oracle):
         assert to_int(oracle.mul(a, b)) == A * B
         q, r = oracle.div(a, b)
         assert to_int(q) == A // B and to_int(r) == A % B
+
+
+# Divisions on which the reference's own Newton division breaks its size
+# preconditions and aborts (natural.h:670-676): (seed_a, n_a, seed_b, n_b).
+REFERENCE_ABORTS = [(5046, 7406, 5047, 3703), (19141, 4406, 19142, 2203)]
+
+
+def test_divisions_the_reference_cannot_do_are_exact(oracle):
+    """The oracle detects the broken precondition and finishes with an exact
+    long division; the results are checked against Python integers."""
+    from oracle import to_int
+    for sa, na, sb, nb in REFERENCE_ABORTS:
+        a, b = limbs(sa, na), limbs(sb, nb)
+        q, r = oracle.div(a, b)
+        A, B = to_int(a), to_int(b)
+        assert to_int(q) == A // B and to_int(r) == A % B
