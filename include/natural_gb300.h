@@ -227,6 +227,19 @@ nn_status nn_to_dec_host(nn_context* ctx, const uint64_t* a, uint64_t n_a, char*
 nn_status nn_pi_dec_host(nn_context* ctx, uint64_t terms, uint64_t acc, uint64_t digits, char** out, uint64_t* len);
 nn_status nn_e_dec_host(nn_context* ctx, uint64_t terms, uint64_t digits, char** out, uint64_t* len);
 
+/* The same recipes with the binary-splitting trees and the decimal split tree
+ * evaluated level by level, each level's products as one GPU batch (products
+ * whose shorter operand is below host_below limbs run on host threads).
+ * terms must be a power of two (the trees are then perfect).  timing (8
+ * doubles, may be NULL): total s, tree s, division s, decimal s, GPU-batch s,
+ * host-product s, GPU products, host products. */
+nn_status nn_pi_dec_levels(nn_context* ctx, uint64_t terms, uint64_t acc, uint64_t digits, uint64_t host_below,
+                           char** out, uint64_t* len, double* timing);
+nn_status nn_e_dec_levels(nn_context* ctx, uint64_t terms, uint64_t digits, uint64_t host_below, char** out,
+                          uint64_t* len, double* timing);
+nn_status nn_to_dec_levels(nn_context* ctx, const uint64_t* a, uint64_t n_a, uint64_t host_below, char** out,
+                           uint64_t* len);
+
 #ifdef __cplusplus
 }
 #endif

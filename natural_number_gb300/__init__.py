@@ -106,6 +106,11 @@ def lib() -> C.CDLL:
         "nn_server_get_stats": (C.c_int, [_vp, C.POINTER(ServerStats)]),
         "nn_server_clock": (C.c_double, [_vp]),
         "nn_server_destroy": (C.c_int, [_vp]),
+        "nn_pi_dec_levels": (C.c_int, [_vp, C.c_uint64, C.c_uint64, C.c_uint64, C.c_uint64, C.POINTER(_vp), _u64p,
+                                       C.POINTER(C.c_double)]),
+        "nn_e_dec_levels": (C.c_int, [_vp, C.c_uint64, C.c_uint64, C.c_uint64, C.POINTER(_vp), _u64p,
+                                      C.POINTER(C.c_double)]),
+        "nn_to_dec_levels": (C.c_int, [_vp, _u64p, C.c_uint64, C.c_uint64, C.POINTER(_vp), _u64p]),
         "nn_launch_count": (C.c_uint64, []),
         "nn_profile_enable": (None, [C.c_int]),
         "nn_profile_report": (C.c_uint64, [C.c_char_p, C.c_uint64]),
@@ -273,6 +278,29 @@ class Context:
     def e_dec(self, terms: int, digits: int) -> str:
         p, n = _vp(), C.c_uint64()
         self._check(lib().nn_e_dec_host(self.h, terms, digits, C.byref(p), C.byref(n)), "e_dec")
+        return self._take_str(p, n.value)
+
+    _TIMING = ("total_s", "tree_s", "division_s", "decimal_s", "gpu_batch_s", "host_product_s", "gpu_products",
+               "host_products")
+
+    def pi_dec_levels(self, terms: int, acc: int, digits: int, host_below: int = 128):
+        """pi digits with level-by-level batched trees; returns (digits, timing dict)."""
+        p, n, t = _vp(), C.c_uint64(), (C.c_double * 8)()
+        self._check(lib().nn_pi_dec_levels(self.h, terms, acc, digits, host_below, C.byref(p), C.byref(n), t),
+                    "pi_dec_levels")
+        return self._take_str(p, n.value), dict(zip(self._TIMING, list(t)))
+
+    def e_dec_levels(self, terms: int, digits: int, host_below: int = 128):
+        p, n, t = _vp(), C.c_uint64(), (C.c_double * 8)()
+        self._check(lib().nn_e_dec_levels(self.h, terms, digits, host_below, C.byref(p), C.byref(n), t),
+                    "e_dec_levels")
+        return self._take_str(p, n.value), dict(zip(self._TIMING, list(t)))
+
+    def to_dec_levels(self, a, host_below: int = 128) -> str:
+        a = _np(a)
+        p, n = _vp(), C.c_uint64()
+        self._check(lib().nn_to_dec_levels(self.h, _ptr(a), a.size, host_below, C.byref(p), C.byref(n)),
+                    "to_dec_levels")
         return self._take_str(p, n.value)
 
     # -- device-pointer API ---------------------------------------------------

@@ -124,3 +124,28 @@ def test_random_2n_by_n_divisions(ctx, seed):
         q, r = ctx.div(a, b)
         A, B = to_int(a), to_int(b)
         assert to_int(q) == A // B and to_int(r) == A % B, n
+
+
+@pytest.mark.parametrize("idx", [0, 1, 2, 3])
+def test_pi_levels_golden(ctx, golden, idx):
+    """pi with the level-by-level batched trees equals the reference's digits;
+    host_below=8 sends all but the smallest products to the GPU."""
+    c = golden["pi"][idx]
+    s, t = ctx.pi_dec_levels(c["terms"], c["acc"], c["digits"], host_below=8 if idx < 2 else 128)
+    assert sdig(s) == c["out"]
+    assert t["gpu_products"] > 0
+
+
+@pytest.mark.parametrize("idx", [0, 1, 2, 3])
+def test_e_levels_golden(ctx, golden, idx):
+    c = golden["e"][idx]
+    s, t = ctx.e_dec_levels(c["terms"], c["digits"], host_below=8 if idx < 2 else 128)
+    assert sdig(s) == c["out"]
+
+
+def test_to_dec_levels_golden(ctx, golden):
+    for c in golden["to_dec"]:
+        assert sdig(ctx.to_dec_levels(limbs(c["seed"], c["n"]), host_below=4)) == c["out"]
+    for c in golden["pow"]:
+        p = ctx.pow(np.array([c["base"]], dtype=np.uint64), c["e"])
+        assert sdig(ctx.to_dec_levels(p, host_below=4)) == c["dec"]
