@@ -261,9 +261,9 @@ def main() -> None:
     import natural_number_gb300 as nn
     from natural_number_gb300.synth import limbs
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from natural_number_gb300 import replicas
+    R = replicas.Rank.from_env()
+    world, rank, local = R.world, R.rank, R.local
     torch.cuda.set_device(local)
     dist = None
     if world > 1:
@@ -274,8 +274,9 @@ def main() -> None:
     L = 1 << (args.n_exp + 1)
     ctx = nn.Context(local)
     stream = torch.cuda.current_stream()
-    a = limbs(SEED_A + rank, n)
-    b = limbs(SEED_B + rank, n)
+    seed_a, seed_b = R.seeds(SEED_A, SEED_B)
+    a = limbs(seed_a, n)
+    b = limbs(seed_b, n)
     da = torch.from_numpy(a).to("cuda")
     db = torch.from_numpy(b).to("cuda")
     out = torch.empty(2 * n, dtype=torch.uint64, device="cuda")
@@ -283,8 +284,7 @@ def main() -> None:
     for _ in range(max(args.warmup, 3)):
         ctx.mul_device(out, da, db)
     torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
+    replicas.barrier(dist)
 
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     l0 = nn.launch_count()
@@ -301,12 +301,9 @@ def main() -> None:
     launches = (nn.launch_count() - l0) / args.steps
     ms = start.elapsed_time(stop) / args.steps
     ctx.synchronize()
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        dist.barrier()
-    value = world * 2 * n / (ms / 1e3)
+    ms = replicas.max_over_ranks(ms, dist, "cuda")
+    replicas.barrier(dist)
+    value = replicas.aggregate_rate(2 * n, world, ms)
 
     # spot-check the last product with size-independent modular identities
     prod = out.cpu().numpy()
@@ -322,17 +319,13 @@ def main() -> None:
         ho = torch.empty(2 * n, dtype=torch.uint64).pin_memory().numpy()
         for _ in range(2):
             ctx.mul(ha, hb, out=ho)
-        if dist:
-            dist.barrier()
+        replicas.barrier(dist)
         t0 = time.perf_counter()
         for _ in range(args.steps):
             ctx.mul(ha, hb, out=ho)
         e_ms = (time.perf_counter() - t0) / args.steps * 1e3
-        if dist:
-            t = torch.tensor([e_ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e_ms = float(t.item())
-        e2e = {"value": world * 2 * n / (e_ms / 1e3), "unit": UNIT, "ms_per_step": e_ms,
+        e_ms = replicas.max_over_ranks(e_ms, dist, "cuda")
+        e2e = {"value": replicas.aggregate_rate(2 * n, world, e_ms), "unit": UNIT, "ms_per_step": e_ms,
                "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 16 * n}
 
     batched = None
