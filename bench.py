@@ -183,6 +183,54 @@ def measure_batched(ctx, steps: int, warmup: int, count: int = 4096) -> dict:
     return out
 
 
+def measure_square(ctx, da, n: int, steps: int, warmup: int) -> dict:
+    """The 2^n-limb square of the benchmark operand (one transform, the
+    fused pass squares), device-resident, CUDA-event timed."""
+    import torch
+    out = torch.empty(2 * n, dtype=torch.uint64, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(max(warmup, 3)):
+        ctx.sqr_device(out, da)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    for _ in range(steps):
+        ctx.sqr_device(out, da)
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / steps
+    L = 2 * n
+    sqr_bytes = 24.0 * n + 96.0 * L
+    peak, _ = peaks()
+    del out
+    return {"ms_per_step": ms, "limbs_per_s": 2 * n / (ms / 1e3), "algorithmic_bytes": sqr_bytes,
+            "frac": sqr_bytes / (ms / 1e3) / 1e9 / peak}
+
+
+def measure_series(ctx) -> dict:
+    """pi and e to 10^8 digits (the reference's test.cpp recipes: pi with
+    2^23 terms and a 6e6-limb square root, e with 2^24 terms), trees
+    evaluated level by level with each level's products batched on the GPU;
+    the digit strings are compared with the reference's SHA-256 digests."""
+    import hashlib
+    golden = json.load(open(os.path.join(ROOT, "tests", "golden", "golden.json")))
+    out = {}
+    for name in ("pi", "e"):
+        c = golden["big_" + name][0]
+        t0 = time.perf_counter()
+        if name == "pi":
+            digits, timing = ctx.pi_dec_levels(c["terms"], c["acc"], c["digits"])
+        else:
+            digits, timing = ctx.e_dec_levels(c["terms"], c["digits"])
+        wall = time.perf_counter() - t0
+        out[name] = {"digits": c["digits"], "seconds": wall,
+                     "exact": hashlib.sha256(digits.encode()).hexdigest() == c["out"]["sha256"],
+                     "reference_seconds_x86_1core": c.get("ref_seconds"),
+                     "phases": {k: round(v, 3) for k, v in timing.items()}}
+        del digits
+    return out
+
+
 def cpu_baseline_port() -> dict:
     """The oracle (single-threaded CPU restatement) on one 2^24 x 2^24 product."""
     from natural_number_gb300.synth import limbs
@@ -250,6 +298,7 @@ def main() -> None:
     ap.add_argument("--no-batch", action="store_true", help="skip the uneven-size batch measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the served request stream")
     ap.add_argument("--serve-jobs", type=int, default=300)
+    ap.add_argument("--series", action="store_true", help="also time pi and e to 10^8 digits (about a minute)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -328,6 +377,8 @@ def main() -> None:
         e2e = {"value": replicas.aggregate_rate(2 * n, world, e_ms), "unit": UNIT, "ms_per_step": e_ms,
                "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 16 * n}
 
+    square = measure_square(ctx, da, n, args.steps, args.warmup)
+
     batched = None
     if not args.no_batch:
         batched = measure_batched(ctx, args.steps, args.warmup)
@@ -335,6 +386,8 @@ def main() -> None:
     if not args.no_serve and rank == 0:
         from natural_number_gb300 import serving as serving_mod
         serving = serving_mod.measure(args.serve_jobs)
+
+    series = measure_series(ctx) if args.series and rank == 0 else None
 
     if rank != 0:
         return
@@ -365,8 +418,11 @@ def main() -> None:
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
+    line["square"] = square
     if e2e:
         line["e2e"] = e2e
+    if series:
+        line["series"] = series
     if batched:
         line["batched"] = batched
     if serving:

@@ -49,6 +49,11 @@ nn_status nn_context_use_own_stream(nn_context* ctx);
 void* nn_context_stream(nn_context* ctx);
 /* Waits for the stream and reports any deferred device-side error. */
 nn_status nn_context_synchronize(nn_context* ctx);
+/* Runs the carry lookback's bounded device wait on a status word that nothing
+ * sets, giving up after spin_limit polls: returns NN_ERR_TIMEOUT, and the
+ * context stays usable.  Checks the timeout path without a fault or a hang
+ * (the reference has no device waits). */
+nn_status nn_context_probe_wait(nn_context* ctx, int spin_limit);
 const char* nn_status_string(nn_status s);
 const char* nn_last_error(const nn_context* ctx);
 /* Bytes of device memory the context holds (tables, transforms, scratch). */

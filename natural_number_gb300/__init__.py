@@ -74,6 +74,7 @@ def lib() -> C.CDLL:
         "nn_context_use_own_stream": (C.c_int, [_vp]),
         "nn_context_stream": (_vp, [_vp]),
         "nn_context_synchronize": (C.c_int, [_vp]),
+        "nn_context_probe_wait": (C.c_int, [_vp, C.c_int]),
         "nn_status_string": (C.c_char_p, [C.c_int]),
         "nn_last_error": (C.c_char_p, [_vp]),
         "nn_context_device_bytes": (C.c_uint64, [_vp]),
@@ -200,6 +201,11 @@ class Context:
 
     def synchronize(self) -> None:
         self._check(lib().nn_context_synchronize(self.h), "synchronize")
+
+    def probe_wait(self, spin_limit: int = 1000) -> int:
+        """Runs the carry lookback's bounded wait on a status word nothing
+        sets; returns the status (NN_ERR_TIMEOUT when the wait gave up)."""
+        return lib().nn_context_probe_wait(self.h, spin_limit)
 
     def device_bytes(self) -> int:
         return lib().nn_context_device_bytes(self.h)

@@ -78,6 +78,12 @@ __global__ void __launch_bounds__(1024) wrap_fix_kernel(u64* out, u64 L, const u
   }
 }
 
+// The lookback's bounded wait on a status word that nothing sets: after
+// `limit` polls it gives up and records the error, as a scan tile does.
+__global__ void wait_probe_kernel(const u32* flag, u32* err, int limit) {
+  if (threadIdx.x == 0 && wait_flag(flag, limit) == 0) atomicExch(err, 1u);
+}
+
 template <class Prod>
 cudaError_t run_scan(const Prod& prod, u64 total, u64* out, u64 out_limit, Scan& sc, cudaStream_t st,
                      const char* name) {
@@ -155,6 +161,17 @@ cudaError_t add_shifted(const u64* x, u64 nx, const u64* y, u64 ny, u64 shift, u
   cudaError_t e = scan_reserve(sc, 1);
   if (e != cudaSuccess) return e;
   return run_scan(AddProducer{x, nx, y, ny, shift}, n, out, n, sc, st, "add_scan");
+}
+
+cudaError_t wait_probe(Scan& sc, int limit, cudaStream_t st) {
+  cudaError_t e = scan_reserve(sc, 1);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(sc.flags, 0, sizeof(u32), st);
+  if (e != cudaSuccess) return e;
+  launch_begin("wait_probe", st);
+  wait_probe_kernel<<<1, 32, 0, st>>>(sc.flags, sc.err, limit);
+  launch_end(st);
+  return cudaGetLastError();
 }
 
 }  // namespace nn

@@ -574,6 +574,12 @@ nn_status nn_context_synchronize(nn_context* c) {
   return NN_OK;
 }
 
+nn_status nn_context_probe_wait(nn_context* c, int spin_limit) {
+  if (!c || spin_limit < 0) return NN_ERR_INVALID;
+  NN_CK(c, nn::wait_probe(c->scan, spin_limit, c->stream), "wait probe");
+  return nn_context_synchronize(c);
+}
+
 const char* nn_last_error(const nn_context* c) { return c ? c->err.c_str() : "no context"; }
 
 uint64_t nn_context_device_bytes(const nn_context* c) {

@@ -110,6 +110,10 @@ cudaError_t school_mul(const u64* a, u64 na, const u64* b, u64 nb, u64* out, Sca
 cudaError_t add_shifted(const u64* x, u64 nx, const u64* y, u64 ny, u64 shift, u64* out, u64 n, Scan& sc,
                         cudaStream_t st);
 
+// Runs the carry lookback's bounded wait on a status word nothing sets (at
+// most `limit` polls); it gives up and sets sc.err, which the host reads.
+cudaError_t wait_probe(Scan& sc, int limit, cudaStream_t st);
+
 // Launch accounting (profile.cpp): every launch site brackets its kernel.
 void launch_begin(const char* name, cudaStream_t st);
 void launch_end(cudaStream_t st);

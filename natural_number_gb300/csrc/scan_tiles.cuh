@@ -143,6 +143,16 @@ __device__ __forceinline__ u32 flag_load(const u32* f) {
 __device__ __forceinline__ void flag_store(u32* f, u32 v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(f), "r"(v) : "memory");
 }
+// Polls *f until it is nonzero, at most `limit` times; 0 means the wait gave up.
+__device__ __forceinline__ u32 wait_flag(const u32* f, int limit) {
+  u32 v;
+  int spins = 0;
+  while ((v = flag_load(f)) == 0) {
+    if (++spins > limit) break;
+    __nanosleep(32);
+  }
+  return v;
+}
 
 // One tile of the scan over positions [0, total): limbs below out_limit go to
 // out, the rest to side.  Tiles of one scan must start in increasing order
@@ -251,12 +261,7 @@ __device__ __forceinline__ void scan_tile(const Prod& prod, u64 tile, u64 total,
           cin = 0;
           break;
         }
-        u32 f;
-        int spins = 0;
-        while ((f = flag_load(&flags[j])) == 0) {
-          if (++spins > kSpinLimit) break;
-          __nanosleep(32);
-        }
+        const u32 f = wait_flag(&flags[j], kSpinLimit);
         if (f == 0) {
           atomicExch(err, 1u);
           cin = 0;
