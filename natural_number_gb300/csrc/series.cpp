@@ -4,19 +4,28 @@
 // natural.h:841-902) and its decimal output (_dec_split/_format_dec,
 // natural.h:953-1011) recursively, one product at a time.  For a number of
 // terms that is a power of two both recursion trees are perfect, so here they
-// are evaluated level by level with the same node formulas: every product of
-// one level is independent, and the level's products go to the GPU as one
-// batch (nn_batch_create/nn_batch_launch, the persistent work-queue kernel).
-// Products whose shorter operand is below `host_below` limbs (the bottom
-// levels: millions of products of a few limbs) run on host threads with a
-// schoolbook loop.  The values are the reference's: products are exact
-// whichever way they are computed, and the adds, |a - b| subtractions, shifts
-// and correction loops between them are the reference's own steps.
+// are evaluated with the same node formulas in two parts:
+//  - the bottom of each tree (subtrees whose values stay below `host_below`
+//    limbs: millions of products of a few limbs) runs on host threads, one
+//    whole subtree per task, on flat limb spans in per-thread scratch (no
+//    allocation per node);
+//  - the levels above run level by level: every product of one level is
+//    independent, and the level's products go to the GPU as one batch
+//    (nn_batch_create/nn_batch_launch, the persistent work-queue kernel)
+//    through pinned staging buffers.
+// The values are the reference's: products are exact whichever way they are
+// computed, and the adds, |a - b| subtractions, shifts and correction loops
+// between them are the reference's own steps.
 #include <cuda_runtime.h>
+#include <sched.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
+#include <cstdio>
 #include <cstring>
+#include <exception>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -27,51 +36,188 @@
 namespace {
 
 using u64 = uint64_t;
+using u128 = unsigned __int128;
 using Clock = std::chrono::steady_clock;
 
-// Host schoolbook product of small naturals (normalised result).
-natural host_mul(const natural& a, const natural& b) {
-  natural d;
-  d.resize(a.size + b.size);
-  std::memset(d.data, 0, 8 * d.size);
-  for (u64 i = 0; i < a.size; ++i) {
-    unsigned __int128 c = 0;
-    const u64 x = a[i];
-    if (!x) continue;
-    for (u64 j = 0; j < b.size; ++j) {
-      c += (unsigned __int128)x * b[j] + d[i + j];
-      d[i + j] = (u64)c;
-      c >>= 64;
+double since(Clock::time_point t) { return std::chrono::duration<double>(Clock::now() - t).count(); }
+
+// ---------------------------------------------------------------------------
+// Host threads
+// ---------------------------------------------------------------------------
+
+// Usable cores: the affinity mask, capped by a cgroup v2 CPU quota if one is set.
+unsigned host_threads() {
+  static const unsigned n = [] {
+    unsigned c = std::thread::hardware_concurrency();
+    if (c == 0) c = 1;
+    cpu_set_t set;
+    if (sched_getaffinity(0, sizeof set, &set) == 0) c = std::min<unsigned>(c, (unsigned)CPU_COUNT(&set));
+    if (FILE* f = std::fopen("/sys/fs/cgroup/cpu.max", "r")) {
+      char quota[32] = {0};
+      unsigned long long period = 0;
+      if (std::fscanf(f, "%31s %llu", quota, &period) == 2 && std::strcmp(quota, "max") != 0 && period) {
+        const unsigned long long q = std::strtoull(quota, nullptr, 10);
+        c = std::min<unsigned>(c, (unsigned)std::max<unsigned long long>(1, (q + period - 1) / period));
+      }
+      std::fclose(f);
     }
-    d[i + b.size] = (u64)c;
-  }
-  return d.std();
+    return std::max(1u, std::min(c, 128u));
+  }();
+  return n;
 }
 
+// f(i) for i in [0, n), threads taking blocks of `grain` indices in turn; the
+// first exception thrown by any task is rethrown here.
 template <class F>
-void parallel_for(u64 n, F&& f) {
-  const unsigned hw = std::max(1u, std::min(std::thread::hardware_concurrency(), 64u));
-  if (n < 256 || hw == 1) {
+void parallel_for(u64 n, u64 grain, F&& f) {
+  grain = std::max<u64>(grain, 1);
+  const unsigned T = (unsigned)std::min<u64>(host_threads(), (n + grain - 1) / grain);
+  if (T <= 1) {
     for (u64 i = 0; i < n; ++i) f(i);
     return;
   }
+  std::atomic<u64> next{0};
+  std::exception_ptr err;
+  std::mutex mu;
+  auto work = [&] {
+    try {
+      for (;;) {
+        const u64 i0 = next.fetch_add(grain);
+        if (i0 >= n) break;
+        const u64 i1 = std::min(n, i0 + grain);
+        for (u64 i = i0; i < i1; ++i) f(i);
+      }
+    } catch (...) {
+      std::lock_guard<std::mutex> g(mu);
+      if (!err) err = std::current_exception();
+      next.store(n);
+    }
+  };
   std::vector<std::thread> ts;
-  for (unsigned t = 0; t < hw; ++t)
-    ts.emplace_back([&, t] {
-      for (u64 i = t; i < n; i += hw) f(i);
-    });
+  ts.reserve(T - 1);
+  for (unsigned t = 1; t < T; ++t) ts.emplace_back(work);
+  work();
   for (auto& th : ts) th.join();
+  if (err) std::rethrow_exception(err);
 }
 
-struct Products {
-  std::vector<const natural*> a, b;
-  std::vector<natural*> out;
-  void add(natural* o, const natural* x, const natural* y) {
-    a.push_back(x);
-    b.push_back(y);
-    out.push_back(o);
+// ---------------------------------------------------------------------------
+// Limb spans (little-endian u64; length 0 is the value 0)
+// ---------------------------------------------------------------------------
+
+inline u64 norm(const u64* a, u64 n) {
+  while (n && a[n - 1] == 0) --n;
+  return n;
+}
+
+// out[0..na+nb) = a * b (schoolbook); returns the normalised length.  out
+// must not overlap a or b.
+u64 mul_span(u64* out, const u64* a, u64 na, const u64* b, u64 nb) {
+  if (!na || !nb) return 0;
+  if (na < nb) {
+    std::swap(a, b);
+    std::swap(na, nb);
   }
-};
+  std::memset(out, 0, 8 * (na + nb));
+  for (u64 j = 0; j < nb; ++j) {
+    const u64 bj = b[j];
+    u64* o = out + j;
+    u64 c = 0;
+    for (u64 i = 0; i < na; ++i) {
+      const u128 t = (u128)a[i] * bj + o[i] + c;
+      o[i] = (u64)t;
+      c = (u64)(t >> 64);
+    }
+    o[na] = c;
+  }
+  return norm(out, na + nb);
+}
+
+// out = a + b; out may be a or b (it needs max(na, nb) + 1 words).
+u64 add_span(u64* out, const u64* a, u64 na, const u64* b, u64 nb) {
+  if (na < nb) {
+    std::swap(a, b);
+    std::swap(na, nb);
+  }
+  u64 c = 0;
+  for (u64 i = 0; i < nb; ++i) {
+    const u128 t = (u128)a[i] + b[i] + c;
+    out[i] = (u64)t;
+    c = (u64)(t >> 64);
+  }
+  for (u64 i = nb; i < na; ++i) {
+    const u64 t = a[i] + c;
+    c = t < c;
+    out[i] = t;
+  }
+  out[na] = c;
+  return norm(out, na + 1);
+}
+
+int cmp_span(const u64* a, u64 na, const u64* b, u64 nb) {
+  if (na != nb) return na < nb ? -1 : 1;
+  for (u64 i = na; i-- > 0;)
+    if (a[i] != b[i]) return a[i] < b[i] ? -1 : 1;
+  return 0;
+}
+
+// out = a - b for a >= b (normalised lengths); out may be a or b.
+u64 sub_span(u64* out, const u64* a, u64 na, const u64* b, u64 nb) {
+  u64 br = 0;
+  for (u64 i = 0; i < nb; ++i) {
+    const u64 x = a[i], y = b[i];
+    out[i] = x - y - br;
+    br = (x < y) | ((x == y) & br);
+  }
+  for (u64 i = nb; i < na; ++i) {
+    const u64 x = a[i];
+    out[i] = x - br;
+    br = x < br;
+  }
+  return norm(out, na);
+}
+
+// |a - b| as natural::operator- computes it (natural.h:324-343); out may be a or b.
+u64 absdiff_span(u64* out, const u64* a, u64 na, const u64* b, u64 nb) {
+  return cmp_span(a, na, b, nb) >= 0 ? sub_span(out, a, na, b, nb) : sub_span(out, b, nb, a, na);
+}
+
+// out = a >> bits; out may be a.
+u64 shr_span(u64* out, const u64* a, u64 na, u64 bits) {
+  const u64 w = bits >> 6, s = bits & 63;
+  if (w >= na) return 0;
+  const u64 n = na - w;
+  if (s == 0) {
+    std::memmove(out, a + w, 8 * n);
+  } else {
+    for (u64 i = 0; i + 1 < n; ++i) out[i] = (a[w + i] >> s) | (a[w + i + 1] << (64 - s));
+    out[n - 1] = a[w + n - 1] >> s;
+  }
+  return norm(out, n);
+}
+
+natural to_natural(const u64* a, u64 n) {
+  natural x;
+  x.resize(std::max<u64>(n, 1));
+  if (n)
+    std::memcpy(x.data, a, 8 * n);
+  else
+    x.data[0] = 0;
+  return x.std();
+}
+
+inline u64 span_len(const natural& x) { return (x.size == 1 && x.data[0] == 0) ? 0 : x.size; }
+
+// Per-thread scratch, grown on demand and kept for the thread's lifetime.
+u64* scratch_words(u64 words) {
+  static thread_local std::vector<u64> buf;
+  if (buf.size() < words) buf.resize(words);
+  return buf.data();
+}
+
+// ---------------------------------------------------------------------------
+// GPU batches of products through pinned staging
+// ---------------------------------------------------------------------------
 
 struct Stats {
   double gpu_s = 0, host_s = 0;
@@ -82,125 +228,267 @@ void check_cuda(cudaError_t e, const char* what) {
   if (e != cudaSuccess) throw std::runtime_error(std::string("natural_gb300: ") + what + ": " + cudaGetErrorString(e));
 }
 
-// Computes every product of P: small ones on host threads, the rest as one GPU batch.
-void run_products(nn_context* c, Products& P, u64 host_below, Stats& S) {
-  std::vector<u64> host, gpu;
-  for (u64 k = 0; k < P.out.size(); ++k)
-    (std::min(P.a[k]->size, P.b[k]->size) < host_below ? host : gpu).push_back(k);
-  auto t0 = Clock::now();
-  parallel_for(host.size(), [&](u64 i) {
-    const u64 k = host[i];
-    natural r = host_mul(*P.a[k], *P.b[k]);
-    *P.out[k] = std::move(r);
-  });
-  auto t1 = Clock::now();
-  S.host_s += std::chrono::duration<double>(t1 - t0).count();
-  S.host_products += host.size();
-  if (gpu.empty()) return;
-  // pack operands, run one batch, unpack
-  std::vector<u64> na(gpu.size()), nb(gpu.size()), oa(gpu.size()), ob(gpu.size()), oo(gpu.size());
-  u64 tin = 0, tout = 0;
-  for (u64 i = 0; i < gpu.size(); ++i) {
-    const u64 k = gpu[i];
-    na[i] = P.a[k]->size;
-    nb[i] = P.b[k]->size;
-    oa[i] = tin;
-    tin += na[i];
-    ob[i] = tin;
-    tin += nb[i];
-    oo[i] = tout;
-    tout += na[i] + nb[i];
+// Grow-only pinned host buffer.
+struct Pinned {
+  u64* p = nullptr;
+  u64 cap = 0;
+  u64* get(u64 words) {
+    if (words > cap) {
+      if (p) cudaFreeHost(p);
+      p = nullptr;
+      cap = 0;
+      const u64 w = std::max<u64>(words + words / 4, 1 << 16);
+      check_cuda(cudaHostAlloc((void**)&p, 8 * w, cudaHostAllocDefault), "pinned staging");
+      cap = w;
+    }
+    return p;
   }
-  std::vector<u64> hin(tin), hout(tout);
-  parallel_for(gpu.size(), [&](u64 i) {
-    const u64 k = gpu[i];
-    std::memcpy(hin.data() + oa[i], P.a[k]->data, 8 * na[i]);
-    std::memcpy(hin.data() + ob[i], P.b[k]->data, 8 * nb[i]);
+  Pinned() = default;
+  Pinned(const Pinned&) = delete;
+  Pinned& operator=(const Pinned&) = delete;
+  ~Pinned() {
+    if (p) cudaFreeHost(p);
+  }
+};
+
+struct Staging {
+  Pinned in, out;
+};
+
+// Products out[k] = a[k] * b[k] of nonzero naturals, computed as one batch on the GPU.
+struct Products {
+  std::vector<const natural*> a, b;
+  std::vector<natural*> out;
+  void add(natural* o, const natural* x, const natural* y) {
+    a.push_back(x);
+    b.push_back(y);
+    out.push_back(o);
+  }
+  u64 size() const { return out.size(); }
+};
+
+void run_products(nn_context* c, Products& P, Staging& stg, Stats& S) {
+  const u64 m = P.size();
+  if (!m) return;
+  const auto t0 = Clock::now();
+  std::vector<u64> na(m), nb(m), oa(m), ob(m), oo(m);
+  u64 tin = 0, tout = 0;
+  for (u64 k = 0; k < m; ++k) {
+    na[k] = P.a[k]->size;
+    nb[k] = P.b[k]->size;
+    oa[k] = tin;
+    tin += na[k];
+    ob[k] = tin;
+    tin += nb[k];
+    oo[k] = tout;
+    tout += na[k] + nb[k];
+  }
+  u64* hin = stg.in.get(tin);
+  u64* hout = stg.out.get(tout);
+  parallel_for(m, 256, [&](u64 k) {
+    std::memcpy(hin + oa[k], P.a[k]->data, 8 * na[k]);
+    std::memcpy(hin + ob[k], P.b[k]->data, 8 * nb[k]);
   });
   cudaStream_t st = (cudaStream_t)nn_context_stream(c);
   u64 *din = nullptr, *dout = nullptr;
   check_cuda(cudaMallocAsync((void**)&din, 8 * tin, st), "batch operands");
   check_cuda(cudaMallocAsync((void**)&dout, 8 * tout, st), "batch products");
-  check_cuda(cudaMemcpyAsync(din, hin.data(), 8 * tin, cudaMemcpyHostToDevice, st), "upload");
-  std::vector<nn_mul_job> jobs(gpu.size());
-  for (u64 i = 0; i < gpu.size(); ++i) jobs[i] = nn_mul_job{din + oa[i], na[i], din + ob[i], nb[i], dout + oo[i]};
+  check_cuda(cudaMemcpyAsync(din, hin, 8 * tin, cudaMemcpyHostToDevice, st), "upload");
+  std::vector<nn_mul_job> jobs(m);
+  for (u64 k = 0; k < m; ++k) jobs[k] = nn_mul_job{din + oa[k], na[k], din + ob[k], nb[k], dout + oo[k]};
   nn_batch* B = nullptr;
-  nn_status s = nn_batch_create(c, na.data(), nb.data(), nullptr, gpu.size(), &B);
+  nn_status s = nn_batch_create(c, na.data(), nb.data(), nullptr, m, &B);
   if (s == NN_OK) s = nn_batch_launch(c, B, jobs.data());
-  if (s == NN_OK) check_cuda(cudaMemcpyAsync(hout.data(), dout, 8 * tout, cudaMemcpyDeviceToHost, st), "download");
+  if (s == NN_OK) check_cuda(cudaMemcpyAsync(hout, dout, 8 * tout, cudaMemcpyDeviceToHost, st), "download");
   if (B) nn_batch_destroy(c, B);
   cudaFreeAsync(din, st);
   cudaFreeAsync(dout, st);
   nn_gb300::check(s == NN_OK ? nn_context_synchronize(c) : s, "batched products");
-  parallel_for(gpu.size(), [&](u64 i) {
-    const u64 k = gpu[i];
-    natural r;
-    r.resize(na[i] + nb[i]);
-    std::memcpy(r.data, hout.data() + oo[i], 8 * r.size);
-    r.std();
-    *P.out[k] = std::move(r);
-  });
-  S.gpu_s += std::chrono::duration<double>(Clock::now() - t1).count();
-  S.gpu_products += gpu.size();
+  parallel_for(m, 64, [&](u64 k) { *P.out[k] = to_natural(hout + oo[k], norm(hout + oo[k], na[k] + nb[k])); });
+  S.gpu_s += since(t0);
+  S.gpu_products += m;
   S.batches += 1;
+}
+
+// ---------------------------------------------------------------------------
+// pi: calc_pi (natural.h:874-902) over terms [1, terms], terms a power of two
+// ---------------------------------------------------------------------------
+
+// Capacities (limbs) of a node covering c terms: a leaf's den and numc take at
+// most 4 limbs and its num at most 6; a parent's den and numc are products of
+// its children's, its num a sum (or difference) of two products.
+inline u64 pi_cap_den(u64 c) { return 4 * c; }
+inline u64 pi_cap_numc(u64 c) { return 4 * c; }
+inline u64 pi_cap_num(u64 c) { return 4 * c + 72; }
+u64 pi_scratch(u64 c) {
+  if (c == 1) return 32;
+  const u64 h = c / 2;
+  return 2 * (pi_cap_num(h) + pi_cap_den(h) + pi_cap_numc(h)) + 2 * pi_cap_num(c) + pi_scratch(h);
+}
+
+struct Len3 {
+  u64 num, den, numc;
+};
+
+// Terms [b, b + c), c a power of two: num/den/numc of calc_pi(b, b + c).
+Len3 pi_subtree(u64 b, u64 c, u64* num, u64* den, u64* numc, u64* tmp) {
+  if (c == 1) {  // natural.h:875-884
+    const u64 one_b[1] = {b};
+    u64* t = tmp;
+    u64 n = mul_span(t, one_b, 1, one_b, 1);
+    const u64 n2 = mul_span(t + 4, t, n, one_b, 1);
+    const u64 k0[1] = {0x26dd041d878000ull};
+    Len3 r;
+    r.den = mul_span(den, t + 4, n2, k0, 1);
+    const u64 f1[1] = {2 * b - 1}, f2[1] = {6 * b - 1}, f3[1] = {6 * b - 5};
+    n = mul_span(t, f1, 1, f2, 1);
+    r.numc = mul_span(numc, t, n, f3, 1);
+    const u64 k1[1] = {0x207e2da6ull}, k2[1] = {0xcf6371};
+    n = mul_span(t + 8, k1, 1, one_b, 1);
+    n = add_span(t + 8, t + 8, n, k2, 1);
+    r.num = mul_span(num, t + 8, n, numc, r.numc);
+    return r;
+  }
+  const u64 h = c / 2;
+  u64* Ln = tmp;
+  u64* Ld = Ln + pi_cap_num(h);
+  u64* Lc = Ld + pi_cap_den(h);
+  u64* Rn = Lc + pi_cap_numc(h);
+  u64* Rd = Rn + pi_cap_num(h);
+  u64* Rc = Rd + pi_cap_den(h);
+  u64* t1 = Rc + pi_cap_numc(h);
+  u64* t2 = t1 + pi_cap_num(c);
+  u64* rest = t2 + pi_cap_num(c);
+  const Len3 L = pi_subtree(b, h, Ln, Ld, Lc, rest);
+  const Len3 R = pi_subtree(b + h, h, Rn, Rd, Rc, rest);
+  Len3 out;
+  if (c == 2) {  // natural.h:888-893: num = |numc * num1 - num * den1|
+    const u64 n1 = mul_span(t1, Lc, L.numc, Rn, R.num);
+    const u64 n2 = mul_span(t2, Ln, L.num, Rd, R.den);
+    out.num = absdiff_span(t1, t1, n1, t2, n2);
+    std::memcpy(num, t1, 8 * out.num);
+  } else {  // natural.h:894-900: num = den1 * num + numc * num1
+    const u64 n1 = mul_span(t1, Rd, R.den, Ln, L.num);
+    const u64 n2 = mul_span(t2, Lc, L.numc, Rn, R.num);
+    out.num = add_span(num, t1, n1, t2, n2);
+  }
+  out.den = mul_span(den, Rd, R.den, Ld, L.den);
+  out.numc = mul_span(numc, Lc, L.numc, Rc, R.numc);
+  return out;
 }
 
 struct PiNode {
   natural num, den, numc;
 };
 
-// calc_pi(num, den, numc, 1, terms + 1) (natural.h:874-902) for terms a power of two.
-void calc_pi_levels(nn_context* c, u64 terms, natural& num, natural& den, natural& numc, u64 host_below, Stats& S) {
-  std::vector<PiNode> lv(terms);
-  parallel_for(terms, [&](u64 i) {  // leaves (natural.h:875-884)
-    const u64 b = i + 1;
-    PiNode& n = lv[i];
-    n.den = host_mul(host_mul(host_mul(natural(b), natural(b)), natural(b)), natural(0x26dd041d878000ull));
-    n.numc = host_mul(host_mul(natural(2 * b - 1), natural(6 * b - 1)), natural(6 * b - 5));
-    n.num = host_mul(host_mul(natural(0x207e2da6ull), natural(b)) + natural(0xcf6371), n.numc);
+void calc_pi_levels(nn_context* c, u64 terms, natural& num, natural& den, natural& numc, u64 host_below,
+                    Staging& stg, Stats& S) {
+  // subtrees of `chunk` terms on the host: their den reaches about host_below limbs
+  const u64 chunk = std::min(std::bit_floor(std::max<u64>(2, host_below / 2)), terms);
+  const u64 nodes = terms / chunk;
+  std::vector<PiNode> lv(nodes);
+  const auto t0 = Clock::now();
+  parallel_for(nodes, 1, [&](u64 k) {
+    const u64 cn = pi_cap_num(chunk), cd = pi_cap_den(chunk), cc = pi_cap_numc(chunk);
+    u64* w = scratch_words(cn + cd + cc + pi_scratch(chunk));
+    const Len3 r = pi_subtree(1 + k * chunk, chunk, w, w + cn, w + cn + cd, w + cn + cd + cc);
+    lv[k].num = to_natural(w, r.num);
+    lv[k].den = to_natural(w + cn, r.den);
+    lv[k].numc = to_natural(w + cn + cd, r.numc);
   });
-  bool pair_level = true;  // end - begin == 2 (natural.h:888-893)
-  while (lv.size() > 1) {
+  S.host_s += since(t0);
+  S.host_products += terms * 6 + (terms - nodes) * 4;
+  while (lv.size() > 1) {  // every level above the host subtrees (end - begin > 2)
     const u64 m = lv.size() / 2;
     std::vector<PiNode> up(m);
     std::vector<natural> t1(m), t2(m);
     Products P;
     for (u64 j = 0; j < m; ++j) {
       PiNode &L = lv[2 * j], &R = lv[2 * j + 1];
-      if (pair_level) {
-        P.add(&t1[j], &L.numc, &R.num);  // numc * num1
-        P.add(&t2[j], &L.num, &R.den);   // num * den1
-      } else {
-        P.add(&t1[j], &R.den, &L.num);    // num = den1 * num
-        P.add(&t2[j], &L.numc, &R.num);   // num1 = numc * num1
-      }
+      P.add(&t1[j], &R.den, &L.num);          // num = den1 * num
+      P.add(&t2[j], &L.numc, &R.num);         // num1 = numc * num1
       P.add(&up[j].den, &R.den, &L.den);      // den = den1 * den
       P.add(&up[j].numc, &L.numc, &R.numc);   // numc = numc * numc1
     }
-    run_products(c, P, host_below, S);
-    parallel_for(m, [&](u64 j) {
-      up[j].num = pair_level ? t1[j] - t2[j] : t1[j] + t2[j];  // |a - b| as natural::operator-
-    });
+    run_products(c, P, stg, S);
+    parallel_for(m, 64, [&](u64 j) { up[j].num = t1[j] + t2[j]; });
+    std::vector<PiNode> old;
+    old.swap(lv);
     lv.swap(up);
-    pair_level = false;
+    parallel_for(old.size(), 256, [&](u64 k) { PiNode dead = std::move(old[k]); });
   }
   num = std::move(lv[0].num);
   den = std::move(lv[0].den);
   numc = std::move(lv[0].numc);
 }
 
+// ---------------------------------------------------------------------------
+// e: calc_e (natural.h:841-857) over [0, terms), terms a power of two >= 2
+// ---------------------------------------------------------------------------
+
+// A node of c pairs: den at most 2c limbs, num at most 2c + log2(c) + 1.
+inline u64 e_cap_den(u64 c) { return 2 * c + 2; }
+inline u64 e_cap_num(u64 c) { return 2 * c + 66; }
+u64 e_scratch(u64 c) {
+  if (c == 1) return 0;
+  const u64 h = c / 2;
+  return 2 * (e_cap_num(h) + e_cap_den(h)) + e_cap_num(c) + e_scratch(h);
+}
+
+struct Len2 {
+  u64 num, den;
+};
+
+// Pairs [i0, i0 + c): pair i is calc_e(2i, 2i + 2).
+Len2 e_subtree(u64 i0, u64 c, u64* num, u64* den, u64* tmp) {
+  if (c == 1) {
+    const u64 b = 2 * i0;
+    num[0] = b + 2;
+    Len2 r{1, 1};
+    if (b) {
+      const u64 x[1] = {b + 1}, y[1] = {b};
+      r.den = mul_span(den, x, 1, y, 1);
+    } else {
+      den[0] = 1;
+    }
+    return r;
+  }
+  const u64 h = c / 2;
+  u64* Ln = tmp;
+  u64* Ld = Ln + e_cap_num(h);
+  u64* Rn = Ld + e_cap_den(h);
+  u64* Rd = Rn + e_cap_num(h);
+  u64* t = Rd + e_cap_den(h);
+  u64* rest = t + e_cap_num(c);
+  const Len2 L = e_subtree(i0, h, Ln, Ld, rest);
+  const Len2 R = e_subtree(i0 + h, h, Rn, Rd, rest);
+  Len2 out;
+  const u64 nt = mul_span(t, Rd, R.den, Ln, L.num);  // num = den1 * num + num1
+  out.num = add_span(num, t, nt, Rn, R.num);
+  out.den = mul_span(den, Rd, R.den, Ld, L.den);  // den = den1 * den
+  return out;
+}
+
 struct ENode {
   natural num, den;
 };
 
-// calc_e(num, den, 0, terms) (natural.h:841-857) for terms a power of two >= 2.
-void calc_e_levels(nn_context* c, u64 terms, natural& num, natural& den, u64 host_below, Stats& S) {
-  std::vector<ENode> lv(terms / 2);
-  parallel_for(lv.size(), [&](u64 i) {  // leaves [begin, begin + 2)
-    const u64 b = 2 * i;
-    lv[i].num = natural(b + 2);
-    lv[i].den = b ? host_mul(natural(b + 1), natural(b)) : natural(b + 1);
+void calc_e_levels(nn_context* c, u64 terms, natural& num, natural& den, u64 host_below, Staging& stg,
+                   Stats& S) {
+  const u64 pairs = terms / 2;
+  const u64 chunk = std::min(std::bit_floor(std::max<u64>(1, host_below / 2)), pairs);
+  const u64 nodes = pairs / chunk;
+  std::vector<ENode> lv(nodes);
+  const auto t0 = Clock::now();
+  parallel_for(nodes, 1, [&](u64 k) {
+    const u64 cn = e_cap_num(chunk), cd = e_cap_den(chunk);
+    u64* w = scratch_words(cn + cd + e_scratch(chunk));
+    const Len2 r = e_subtree(k * chunk, chunk, w, w + cn, w + cn + cd);
+    lv[k].num = to_natural(w, r.num);
+    lv[k].den = to_natural(w + cn, r.den);
   });
+  S.host_s += since(t0);
+  S.host_products += pairs + (pairs - nodes) * 2;
   while (lv.size() > 1) {
     const u64 m = lv.size() / 2;
     std::vector<ENode> up(m);
@@ -211,42 +499,126 @@ void calc_e_levels(nn_context* c, u64 terms, natural& num, natural& den, u64 hos
       P.add(&t[j], &R.den, &L.num);       // num = den1 * num
       P.add(&up[j].den, &R.den, &L.den);  // den = den1 * den
     }
-    run_products(c, P, host_below, S);
-    parallel_for(m, [&](u64 j) { up[j].num = t[j] + lv[2 * j + 1].num; });
+    run_products(c, P, stg, S);
+    parallel_for(m, 64, [&](u64 j) { up[j].num = t[j] + lv[2 * j + 1].num; });
+    std::vector<ENode> old;
+    old.swap(lv);
     lv.swap(up);
+    parallel_for(old.size(), 256, [&](u64 k) { ENode dead = std::move(old[k]); });
   }
   num = std::move(lv[0].num);
   den = std::move(lv[0].den);
 }
 
-// Decimal digits (std::formatter<natural>, natural.h:1089-1091) with the
-// split tree of _format_dec (natural.h:994-1011) evaluated level by level.
-std::string to_dec_levels(nn_context* c, const natural& x, u64 host_below, Stats& S) {
+// ---------------------------------------------------------------------------
+// Decimal output: _format_dec / _dec_split (natural.h:953-1011)
+// ---------------------------------------------------------------------------
+
+struct DecLevel {  // base[i] = 10^(18 * 2^i), its reciprocal and shift, as spans
+  const u64* base;
+  u64 nb;
+  const u64* base_r;
+  u64 nr;
+  u64 shift;  // ((base.size + 2) << 6) - n_shl
+};
+
+// The split by 10^18 of v < 10^36 (i == 0, natural.h:954-955) and the two
+// 18-digit leaves; the first node omits leading zeros.
+u64 dec_leaf(const u64* v, u64 nv, bool first, char* out) {
+  const u128 x = nv == 0 ? 0 : nv == 1 ? (u128)v[0] : ((u128)v[1] << 64 | v[0]);
+  const u64 q = (u64)(x / nn_gb300::dec_base_0), r = (u64)(x % nn_gb300::dec_base_0);
+  char buf[48];
+  int n;
+  if (first && q == 0)
+    n = std::snprintf(buf, sizeof buf, "%llu", (unsigned long long)r);
+  else if (first)
+    n = std::snprintf(buf, sizeof buf, "%llu%018llu", (unsigned long long)q, (unsigned long long)r);
+  else
+    n = std::snprintf(buf, sizeof buf, "%018llu%018llu", (unsigned long long)q, (unsigned long long)r);
+  std::memcpy(out, buf, n);
+  return (u64)n;
+}
+
+// Scratch words for dec_subtree at level i.
+u64 dec_scratch(const std::vector<DecLevel>& D, int i) {
+  u64 w = 64;
+  for (int k = 1; k <= i; ++k) w += D[k].nr + 5 * D[k].nb + 32;
+  return w;
+}
+
+// Digits of v (v < base[i]^2) split at level i (0: the leaf split) into out;
+// a node that is not first writes exactly 18 * 2^(i+1) digits.  Returns the
+// number of digits written.
+u64 dec_subtree(const std::vector<DecLevel>& D, const u64* v, u64 nv, int i, bool first, char* out, u64* tmp) {
+  if (i == 0) return dec_leaf(v, nv, first, out);
+  const DecLevel& L = D[i];
+  // hi = base_r * (v >> ((base.size - 1) << 6)) >> shift   (natural.h:958-960)
+  const u64 ny = nv > L.nb - 1 ? nv - (L.nb - 1) : 0;
+  u64* hi = tmp;  // nr + nb + 4 words
+  u64 nh = mul_span(hi, L.base_r, L.nr, v + (L.nb - 1), ny);
+  nh = shr_span(hi, hi, nh, L.shift);
+  // lo = |v - base * hi|, then the correction loop (natural.h:961-966)
+  u64* p = hi + L.nr + L.nb + 4;  // 2 nb + 8 words
+  const u64 np = mul_span(p, L.base, L.nb, hi, nh);
+  u64* lo = p + 2 * L.nb + 8;  // 2 nb + 8 words
+  u64 nl = absdiff_span(lo, v, nv, p, np);
+  while (cmp_span(lo, nl, L.base, L.nb) >= 0) {
+    const u64 one[1] = {1};
+    hi[nh] = 0;
+    nh = add_span(hi, hi, nh, one, 1);
+    nl = sub_span(lo, lo, nl, L.base, L.nb);
+  }
+  u64* rest = lo + 2 * L.nb + 8;
+  if (first && nh == 0) return dec_subtree(D, lo, nl, i - 1, true, out, rest);
+  const u64 w = dec_subtree(D, hi, nh, i - 1, first, out, rest);
+  return w + dec_subtree(D, lo, nl, i - 1, false, out + w, rest);
+}
+
+// Decimal digits (std::formatter<natural>, natural.h:1089-1091): the split
+// tree of _format_dec, level by level with GPU batches while the split
+// powers are at least host_below limbs, then whole subtrees on host threads.
+std::string to_dec_levels(nn_context* c, const natural& x, u64 host_below, Staging& stg, Stats& S) {
   using namespace nn_gb300;
   const int top = dec_init(x);
   if (top < 0) return std::to_string(x[0]);
   DecCache& C = dec_cache();
+  std::vector<DecLevel> D(top + 1);
+  for (int i = 1; i <= top; ++i) {
+    const natural& b = C.base[i];
+    const unsigned n_shl = (unsigned)(std::countl_zero(b[b.size - 1]) + 1) & 63;
+    D[i] = DecLevel{b.data, b.size, C.base_r[i].data, C.base_r[i].size, ((b.size + 2) << 6) - n_shl};
+  }
   struct Node {
     natural v;
     bool first;
   };
   std::vector<Node> lv;
   lv.push_back(Node{x, true});
-  for (int i = top; i >= 1; --i) {
+  int i = top;
+  for (; i >= 1 && std::min(D[i].nb, D[i].nr) >= host_below; --i) {
     const natural& base = C.base[i];
     const natural& base_r = C.base_r[i];
-    const unsigned n_shl = (unsigned)(std::countl_zero(base[base.size - 1]) + 1) & 63;
     const u64 n = lv.size();
     std::vector<natural> y(n), hi(n), lo(n), p(n);
-    parallel_for(n, [&](u64 k) { y[k] = lv[k].v >> ((base.size - 1) << 6); });
+    parallel_for(n, 16, [&](u64 k) { y[k] = lv[k].v >> ((base.size - 1) << 6); });
     Products P1;
-    for (u64 k = 0; k < n; ++k) P1.add(&hi[k], &base_r, &y[k]);  // mul_load(hi, base_r, x >> .., ni)
-    run_products(c, P1, host_below, S);
-    parallel_for(n, [&](u64 k) { hi[k] >>= ((base.size + 2) << 6) - n_shl; });
+    for (u64 k = 0; k < n; ++k) {
+      if (y[k] == 0)
+        hi[k] = 0;
+      else
+        P1.add(&hi[k], &base_r, &y[k]);  // mul_load(hi, base_r, x >> .., ni)
+    }
+    run_products(c, P1, stg, S);
+    parallel_for(n, 16, [&](u64 k) { hi[k] >>= D[i].shift; });
     Products P2;
-    for (u64 k = 0; k < n; ++k) P2.add(&p[k], &base, &hi[k]);  // mul_load(lo, base, hi, ni)
-    run_products(c, P2, host_below, S);
-    parallel_for(n, [&](u64 k) {
+    for (u64 k = 0; k < n; ++k) {
+      if (hi[k] == 0)
+        p[k] = 0;
+      else
+        P2.add(&p[k], &base, &hi[k]);  // mul_load(lo, base, hi, ni)
+    }
+    run_products(c, P2, stg, S);
+    parallel_for(n, 16, [&](u64 k) {
       lo[k] = lv[k].v - p[k];
       while (lo[k] >= base) {  // natural.h:962-965
         hi[k] += 1;
@@ -265,23 +637,24 @@ std::string to_dec_levels(nn_context* c, const natural& x, u64 host_below, Stats
     }
     lv.swap(next);
   }
-  // level 0: div_base by 10^18 (natural.h:954-955), then the 18-digit leaves
-  std::vector<std::string> parts(lv.size());
-  parallel_for(lv.size(), [&](u64 k) {
-    natural q;
-    const u64 r = div_base(lv[k].v, dec_base_0, q);
-    char buf[48];
-    if (lv[k].first && q == 0)
-      std::snprintf(buf, sizeof buf, "%llu", (unsigned long long)r);
-    else if (lv[k].first)
-      std::snprintf(buf, sizeof buf, "%llu%018llu", (unsigned long long)q[0], (unsigned long long)r);
-    else
-      std::snprintf(buf, sizeof buf, "%018llu%018llu", (unsigned long long)q[0], (unsigned long long)r);
-    parts[k] = buf;
+  // The rest on host threads: node 0 (the first) may be shorter, every other
+  // node writes exactly 18 * 2^(i+1) digits.
+  const auto t0 = Clock::now();
+  const u64 width = 18ull << (i + 1);
+  const u64 scratch = dec_scratch(D, i);
+  std::string head(width + 64, '\0');
+  {
+    const natural& v0 = lv[0].v;
+    head.resize(dec_subtree(D, v0.data, span_len(v0), i, lv[0].first, head.data(), scratch_words(scratch)));
+  }
+  std::string out(head.size() + (lv.size() - 1) * width, '\0');
+  std::memcpy(out.data(), head.data(), head.size());
+  char* body = out.data() + head.size();
+  parallel_for(lv.size() - 1, 1, [&](u64 k) {
+    const natural& v = lv[k + 1].v;
+    dec_subtree(D, v.data, span_len(v), i, false, body + k * width, scratch_words(scratch));
   });
-  std::string out;
-  out.reserve(parts.size() * 36);
-  for (auto& s : parts) out += s;
+  S.host_s += since(t0);
   return out;
 }
 
@@ -300,8 +673,6 @@ void fill_timing(double* t, const double* v, int k) {
     for (int i = 0; i < k; ++i) t[i] = v[i];
 }
 
-double since(Clock::time_point t) { return std::chrono::duration<double>(Clock::now() - t).count(); }
-
 }  // namespace
 
 extern "C" {
@@ -312,9 +683,10 @@ nn_status nn_pi_dec_levels(nn_context* c, uint64_t terms, uint64_t acc, uint64_t
   nn_gb300::ScopedContext scope(c);
   try {
     Stats S;
-    auto t0 = Clock::now();
+    Staging stg;
+    const auto t0 = Clock::now();
     natural num, den, numc, denc;
-    calc_pi_levels(c, terms, num, den, numc, host_below, S);  // test.cpp:22-32 recipe
+    calc_pi_levels(c, terms, num, den, numc, host_below, stg, S);  // test.cpp:22-32 recipe
     const double t_tree = since(t0);
     sqrt_10005(numc, denc, acc);
     num = 0xcf6371 * den - num;
@@ -322,13 +694,13 @@ nn_status nn_pi_dec_levels(nn_context* c, uint64_t terms, uint64_t acc, uint64_t
     num *= denc;
     den /= num;
     const double t_div = since(t0) - t_tree;
-    std::string s = to_dec_levels(c, den, host_below, S);
+    std::string s = to_dec_levels(c, den, host_below, stg, S);
     const double t_all = since(t0);
     const double tv[8] = {t_all, t_tree, t_div, t_all - t_tree - t_div, S.gpu_s, S.host_s, (double)S.gpu_products,
                           (double)S.host_products};
     fill_timing(timing, tv, 8);
     *out = export_str(s, len);
-    return NN_OK;
+    return *out ? NN_OK : NN_ERR_OOM;
   } catch (const std::bad_alloc&) {
     return NN_ERR_OOM;
   } catch (const std::exception&) {
@@ -342,20 +714,21 @@ nn_status nn_e_dec_levels(nn_context* c, uint64_t terms, uint64_t digits, uint64
   nn_gb300::ScopedContext scope(c);
   try {
     Stats S;
-    auto t0 = Clock::now();
+    Staging stg;
+    const auto t0 = Clock::now();
     natural num, den;
-    calc_e_levels(c, terms, num, den, host_below, S);  // test.cpp:12-19 recipe
+    calc_e_levels(c, terms, num, den, host_below, stg, S);  // test.cpp:12-19 recipe
     const double t_tree = since(t0);
     num *= pow(natural(10), digits);
     num /= den;
     const double t_div = since(t0) - t_tree;
-    std::string s = to_dec_levels(c, num, host_below, S);
+    std::string s = to_dec_levels(c, num, host_below, stg, S);
     const double t_all = since(t0);
     const double tv[8] = {t_all, t_tree, t_div, t_all - t_tree - t_div, S.gpu_s, S.host_s, (double)S.gpu_products,
                           (double)S.host_products};
     fill_timing(timing, tv, 8);
     *out = export_str(s, len);
-    return NN_OK;
+    return *out ? NN_OK : NN_ERR_OOM;
   } catch (const std::bad_alloc&) {
     return NN_ERR_OOM;
   } catch (const std::exception&) {
@@ -368,13 +741,11 @@ nn_status nn_to_dec_levels(nn_context* c, const uint64_t* a, uint64_t na, uint64
   if (!c || !a || !na || !out || !len) return NN_ERR_INVALID;
   nn_gb300::ScopedContext scope(c);
   try {
-    natural x;
-    x.resize(na);
-    std::memcpy(x.data, a, 8 * na);
-    x.std();
+    const natural x = to_natural(a, na);
     Stats S;
-    *out = export_str(to_dec_levels(c, x, host_below, S), len);
-    return NN_OK;
+    Staging stg;
+    *out = export_str(to_dec_levels(c, x, host_below, stg, S), len);
+    return *out ? NN_OK : NN_ERR_OOM;
   } catch (const std::bad_alloc&) {
     return NN_ERR_OOM;
   } catch (const std::exception&) {
