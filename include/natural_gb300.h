@@ -233,8 +233,9 @@ nn_status nn_pi_dec_host(nn_context* ctx, uint64_t terms, uint64_t acc, uint64_t
 nn_status nn_e_dec_host(nn_context* ctx, uint64_t terms, uint64_t digits, char** out, uint64_t* len);
 
 /* The same recipes with the binary-splitting trees and the decimal split tree
- * evaluated level by level, each level's products as one GPU batch (products
- * whose shorter operand is below host_below limbs run on host threads).
+ * evaluated level by level, each level's products as one GPU batch; the
+ * bottom subtrees, whose values stay below about host_below limbs (256 is a
+ * good choice), run whole on host threads.
  * terms must be a power of two (the trees are then perfect).  timing (8
  * doubles, may be NULL): total s, tree s, division s, decimal s, GPU-batch s,
  * host-product s, GPU products, host products. */

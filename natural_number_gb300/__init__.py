@@ -289,20 +289,20 @@ class Context:
     _TIMING = ("total_s", "tree_s", "division_s", "decimal_s", "gpu_batch_s", "host_product_s", "gpu_products",
                "host_products")
 
-    def pi_dec_levels(self, terms: int, acc: int, digits: int, host_below: int = 128):
+    def pi_dec_levels(self, terms: int, acc: int, digits: int, host_below: int = 256):
         """pi digits with level-by-level batched trees; returns (digits, timing dict)."""
         p, n, t = _vp(), C.c_uint64(), (C.c_double * 8)()
         self._check(lib().nn_pi_dec_levels(self.h, terms, acc, digits, host_below, C.byref(p), C.byref(n), t),
                     "pi_dec_levels")
         return self._take_str(p, n.value), dict(zip(self._TIMING, list(t)))
 
-    def e_dec_levels(self, terms: int, digits: int, host_below: int = 128):
+    def e_dec_levels(self, terms: int, digits: int, host_below: int = 256):
         p, n, t = _vp(), C.c_uint64(), (C.c_double * 8)()
         self._check(lib().nn_e_dec_levels(self.h, terms, digits, host_below, C.byref(p), C.byref(n), t),
                     "e_dec_levels")
         return self._take_str(p, n.value), dict(zip(self._TIMING, list(t)))
 
-    def to_dec_levels(self, a, host_below: int = 128) -> str:
+    def to_dec_levels(self, a, host_below: int = 256) -> str:
         a = _np(a)
         p, n = _vp(), C.c_uint64()
         self._check(lib().nn_to_dec_levels(self.h, _ptr(a), a.size, host_below, C.byref(p), C.byref(n)),
