@@ -37,10 +37,12 @@ struct Pass {
 // r_last: levels of the contiguous (deepest) pass; r_col: most levels of a
 // strided column pass.
 std::vector<Pass> plan_passes(int s, int r_last = 11, int r_col = 9);
-// Shared memory of a pass tile (C << R words, padded two words per 32).
+// Shared memory of a pass tile (C << R words, padded two words per 32); a
+// row pass (C = 2) also stages its 2^R - 1 twiddle pairs.
 inline size_t tile_smem_bytes(int C, int R) {
   const size_t n = (size_t)C << R;
-  return (n + n / 16 + 2) * 8;
+  const size_t tile = ((n + n / 16 + 3) & ~(size_t)1) * 8;  // even words: the twiddles start 16-byte aligned
+  return C == 2 ? tile + (((size_t)1 << R) - 1) * 16 : tile;
 }
 
 // Scratch for the decoupled-lookback carry scan.

@@ -37,6 +37,47 @@ __device__ __forceinline__ u64 barrett_c(U128 t) {
   return r;
 }
 
+// Butterflies with per-prime lazy ranges.  q = hi(y * wp) with the
+// reference's companion wp = floor(w*2^64/p)+1 is floor(y*w/p) or one more for
+// any y < 2^64, so r = y*w - q*p lies in [-p, p) as a signed value.
+//  - p0, p1 (4p < 2^64): forward values live in [0, 4p) and inverse values in
+//    [0, 2p); r + p enters the sums directly (one conditional per butterfly).
+//  - p2 (4p > 2^64): forward values in [0, 2p), inverse values in [0, p), as
+//    in the reference (asmLinux.asm:409-445, 595-630).
+template <int PR>
+__device__ __forceinline__ void fwd_bfly_c(u64& x, u64& y, u64 w, u64 wp) {
+  constexpr u64 p = PrimeC<PR>::p;
+  constexpr u32 ch = PrimeC<PR>::c_hi;
+  if constexpr (PR < 2) {
+    const u64 r = y * w - mul_p(mulhi(y, wp), ch);  // signed, in [-p, p)
+    const u64 xr = x >= 2 * p ? x - 2 * p : x;      // [0, 2p)
+    x = xr + r + p;                                 // [0, 4p)
+    y = xr - r + p;                                 // [0, 4p)
+  } else {
+    fwd_bfly(x, y, w, wp, p, ch);
+  }
+}
+template <int PR>
+__device__ __forceinline__ void inv_bfly_c(u64& x, u64& y, u64 w, u64 wp) {
+  constexpr u64 p = PrimeC<PR>::p;
+  constexpr u32 ch = PrimeC<PR>::c_hi;
+  if constexpr (PR < 2) {
+    const u64 d = x - y + 2 * p;                    // (0, 4p)
+    const u64 sum = x + y;                          // [0, 4p)
+    x = sum >= 2 * p ? sum - 2 * p : sum;           // [0, 2p)
+    y = d * w - mul_p(mulhi(d, wp), ch) + p;        // r in [-p, p) as a signed value; y in [0, 2p)
+  } else {
+    inv_bfly(x, y, w, wp, p, ch);
+  }
+}
+// Any lazy value of prime PR to [0, p).
+template <int PR>
+__device__ __forceinline__ u64 canon_c(u64 x) {
+  constexpr u64 p = PrimeC<PR>::p;
+  if constexpr (PR < 2) x = x >= 2 * p ? x - 2 * p : x;
+  return reduce2p(x, p);
+}
+
 // Shared-memory padding: two words per 32, so pairs of words stay 16-byte
 // aligned (16-byte async copies) while strided accesses of the deep levels
 // spread over the banks.
@@ -57,34 +98,73 @@ __device__ __forceinline__ void st2(u64* p, ulonglong2 v) {
     *q = v;
 }
 
+// 16-byte asynchronous global -> shared copies (L2 only, as .cg loads), so a
+// thread's loads of a tile are all in flight before any of them is waited on.
+__device__ __forceinline__ void cp_async16(u64* smem, const u64* gmem) {
+  const u32 d = (u32)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
+// Words of the padded tile, rounded up to an even count so that the twiddle
+// pairs a row pass (C = 2) keeps after the tile start on a 16-byte boundary.
+__device__ __forceinline__ u32 tile_words(u32 nel) { return (nel + nel / 16 + 3) & ~1u; }
+
+// The twiddle pairs of one tile of a row pass, staged in shared memory: local
+// level j (global level lambda0 + j) uses pairs ksb*2^j + r, r < 2^j, kept at
+// [2^j - 1, 2^(j+1) - 1).  Every deep-level pair is used by one thread only,
+// so staging turns one dependent load per butterfly group into a batch of
+// asynchronous copies at the start of the tile.
+__device__ __forceinline__ void stage_twiddles(u64* tws, const u64* tw, u64 ksb, int R) {
+  const u32 npairs = (1u << R) - 1;
+  for (u32 q = threadIdx.x; q < npairs; q += blockDim.x) {
+    const u32 j = 31 - __clz(q + 1);
+    const u32 r = q + 1 - (1u << j);
+    cp_async16(tws + 2 * q, tw + 2 * ((ksb << j) + r));
+  }
+}
+
 // K levels [l, l+K) of a tile held in shared memory: each thread takes units
-// of 2^K rows of one column and runs the radix-2^K network in registers.
+// of 2^K rows of one column and runs the radix-2^K network in registers.  The
+// unit's rows are S = C * 2^nsub words apart, and the padded index is linear
+// in the row: pad16(x0 + m*S) = pad16(x0) + m*S + 2*floor(m*S/32) for every
+// unit of every tile shape used here, so each row is one add from the first.
 template <int K, int C, bool INV, int PR>
-__device__ __forceinline__ void level_group(u64* sm, int l, int R, u64 ksb, const u64* __restrict__ tw) {
-  constexpr u64 p = PrimeC<PR>::p;
-  constexpr u32 ch = PrimeC<PR>::c_hi;
+__device__ __forceinline__ void level_group(u64* sm, int l, int R, u64 ksb, const u64* __restrict__ tw,
+                                            const u64* tws) {
   const int nsub = R - l - K;
   const u32 units = (u32)C << (R - K);
   const u32 tmask = (1u << nsub) - 1;
+  const u32 S = (u32)C << nsub;
+  auto off = [S](u32 m) { return m * S + (((m * S) >> 5) << 1); };
   const ulonglong2* twv = reinterpret_cast<const ulonglong2*>(tw);
+  const ulonglong2* twsv = reinterpret_cast<const ulonglong2*>(tws);
+  // twiddle pair g of local level l + lv for the unit of block rb
+  auto twiddle = [&](u32 rb, u64 bidx, int lv, int g) -> ulonglong2 {
+    if (C == 2) return twsv[(1u << (l + lv)) - 1 + (rb << lv) + g];
+    return __ldg(twv + ((bidx << lv) + g));
+  };
   for (u32 u = threadIdx.x; u < units; u += blockDim.x) {
     const u32 i = u & (C - 1);
     const u32 v = u / C;
     const u32 rb = v >> nsub;
     const u32 row0 = (rb << (R - l)) + (v & tmask);
     const u64 bidx = (ksb << l) + rb;
+    u64* sp = sm + pad16(row0 * C + i);
     u64 x[1 << K];
 #pragma unroll
-    for (int m = 0; m < (1 << K); ++m) x[m] = sm[pad16(((row0 + ((u32)m << nsub)) * C) + i)];
+    for (int m = 0; m < (1 << K); ++m) x[m] = sp[off(m)];
     if (!INV) {
 #pragma unroll
       for (int lv = 0; lv < K; ++lv) {
         const int half = (1 << K) >> (lv + 1);
 #pragma unroll
         for (int g = 0; g < (1 << lv); ++g) {
-          const ulonglong2 wv = __ldg(twv + ((bidx << lv) + g));
+          const ulonglong2 wv = twiddle(rb, bidx, lv, g);
 #pragma unroll
-          for (int m = 0; m < half; ++m) fwd_bfly(x[g * 2 * half + m], x[g * 2 * half + m + half], wv.x, wv.y, p, ch);
+          for (int m = 0; m < half; ++m) fwd_bfly_c<PR>(x[g * 2 * half + m], x[g * 2 * half + m + half], wv.x, wv.y);
         }
       }
     } else {
@@ -93,14 +173,14 @@ __device__ __forceinline__ void level_group(u64* sm, int l, int R, u64 ksb, cons
         const int half = (1 << K) >> (lv + 1);
 #pragma unroll
         for (int g = 0; g < (1 << lv); ++g) {
-          const ulonglong2 wv = __ldg(twv + ((bidx << lv) + g));
+          const ulonglong2 wv = twiddle(rb, bidx, lv, g);
 #pragma unroll
-          for (int m = 0; m < half; ++m) inv_bfly(x[g * 2 * half + m], x[g * 2 * half + m + half], wv.x, wv.y, p, ch);
+          for (int m = 0; m < half; ++m) inv_bfly_c<PR>(x[g * 2 * half + m], x[g * 2 * half + m + half], wv.x, wv.y);
         }
       }
     }
 #pragma unroll
-    for (int m = 0; m < (1 << K); ++m) sm[pad16(((row0 + ((u32)m << nsub)) * C) + i)] = x[m];
+    for (int m = 0; m < (1 << K); ++m) sp[off(m)] = x[m];
   }
 }
 
@@ -117,23 +197,23 @@ __device__ __forceinline__ int group_cap(int C, int R) {
 }
 
 template <int C, bool INV, int PR>
-__device__ __forceinline__ void run_group(u64* sm, int k, int l, int R, u64 ksb, const u64* tw) {
+__device__ __forceinline__ void run_group(u64* sm, int k, int l, int R, u64 ksb, const u64* tw, const u64* tws) {
   if (k == 3)
-    level_group<3, C, INV, PR>(sm, l, R, ksb, tw);
+    level_group<3, C, INV, PR>(sm, l, R, ksb, tw, tws);
   else if (k == 2)
-    level_group<2, C, INV, PR>(sm, l, R, ksb, tw);
+    level_group<2, C, INV, PR>(sm, l, R, ksb, tw, tws);
   else
-    level_group<1, C, INV, PR>(sm, l, R, ksb, tw);
+    level_group<1, C, INV, PR>(sm, l, R, ksb, tw, tws);
 }
 
 // Forward levels [0, R) of the tile in shared memory.
 template <int C, int PR>
-__device__ __forceinline__ void tile_forward(u64* sm, int R, u64 ksb, const u64* tw) {
+__device__ __forceinline__ void tile_forward(u64* sm, int R, u64 ksb, const u64* tw, const u64* tws) {
   const int cap = group_cap(C, R);
   const int n = (R + cap - 1) / cap;
   for (int g = 0, l = 0; g < n; ++g) {
     const int k = (R - l + (n - g) - 1) / (n - g);
-    run_group<C, false, PR>(sm, k, l, R, ksb, tw);
+    run_group<C, false, PR>(sm, k, l, R, ksb, tw, tws);
     __syncthreads();
     l += k;
   }
@@ -141,26 +221,26 @@ __device__ __forceinline__ void tile_forward(u64* sm, int R, u64 ksb, const u64*
 
 // Inverse levels R-1 .. 0 of the tile in shared memory.
 template <int C, int PR>
-__device__ __forceinline__ void tile_inverse(u64* sm, int R, u64 ksb, const u64* tw) {
+__device__ __forceinline__ void tile_inverse(u64* sm, int R, u64 ksb, const u64* tw, const u64* tws) {
   const int cap = group_cap(C, R);
   const int n = (R + cap - 1) / cap;
   for (int g = 0, l = R; g < n; ++g) {
     const int k = (l + (n - g) - 1) / (n - g);
     l -= k;
-    run_group<C, true, PR>(sm, k, l, R, ksb, tw);
+    run_group<C, true, PR>(sm, k, l, R, ksb, tw, tws);
     __syncthreads();
   }
 }
 
-// Pointwise product of one group of 4 residues (a0..a3)(b0..b3), raw [0,2p)
-// inputs, [0,p) outputs: degree-1 residues mod (x^2 - w) and (x^2 + w),
+// Pointwise product of one group of 4 residues (a0..a3)(b0..b3), lazy forward
+// values as inputs, [0,p) outputs: degree-1 residues mod (x^2 - w) and (x^2 + w),
 // w = root[2g] (ntt_info.h:224-231, asmLinux.asm:910-1057).
 template <int PR>
 __device__ __forceinline__ void pointwise4(u64 (&o)[4], const u64 (&A)[4], const u64 (&Bv)[4], ulonglong2 wv) {
   constexpr u64 p = PrimeC<PR>::p;
   constexpr u32 ch = PrimeC<PR>::c_hi;
-  const u64 a0 = reduce2p(A[0], p), a1 = reduce2p(A[1], p), a2 = reduce2p(A[2], p), a3 = reduce2p(A[3], p);
-  const u64 b0 = reduce2p(Bv[0], p), b1 = reduce2p(Bv[1], p), b2 = reduce2p(Bv[2], p), b3 = reduce2p(Bv[3], p);
+  const u64 a0 = canon_c<PR>(A[0]), a1 = canon_c<PR>(A[1]), a2 = canon_c<PR>(A[2]), a3 = canon_c<PR>(A[3]);
+  const u64 b0 = canon_c<PR>(Bv[0]), b1 = canon_c<PR>(Bv[1]), b2 = canon_c<PR>(Bv[2]), b3 = canon_c<PR>(Bv[3]);
   const u64 wb1 = shoup_mul(b1, wv.x, wv.y, p, ch);
   const u64 wb3 = shoup_mul(b3, wv.x, wv.y, p, ch);
   const u64 nwb3 = wb3 ? p - wb3 : 0;
@@ -211,18 +291,20 @@ __device__ __forceinline__ void pass_tile_p(u64* sm, const u64* in, u64* out, u6
     const u64* src = in + (u64)PR * L;
     for (u32 idx = 2 * threadIdx.x; idx < nel; idx += 2 * blockDim.x) {
       const u64 pos = base + ((u64)(idx >> LGC) << lg_s) + (idx & (C - 1));
-      const ulonglong2 v = ld2<CG>(src + pos);
-      sm[pad16(idx)] = v.x;
-      sm[pad16(idx + 1)] = v.y;
+      cp_async16(sm + pad16(idx), src + pos);
     }
   }
+  u64* tws = sm + tile_words(nel);
+  if (C == 2) stage_twiddles(tws, tw, ksb, R);
+  cp_async_wait_all();
   __syncthreads();
 
   if (!INV) {
-    tile_forward<C, PR>(sm, R, ksb, tw);
+    tile_forward<C, PR>(sm, R, ksb, tw, tws);
     if (FUSED) {  // contiguous tile: smem index == position - base; other == nullptr squares
       const u64* oth = other ? other + (u64)PR * L : nullptr;
-      const ulonglong2* twv = reinterpret_cast<const ulonglong2*>(tw);
+      const ulonglong2* twsv = reinterpret_cast<const ulonglong2*>(tws);
+      const u32 deep = (1u << (R - 1)) - 1;  // local level R-1: the blocks of 4 residues
       for (u32 g4 = 4 * threadIdx.x; g4 < nel; g4 += 4 * blockDim.x) {
         const u64 Bv[4] = {sm[pad16(g4)], sm[pad16(g4 + 1)], sm[pad16(g4 + 2)], sm[pad16(g4 + 3)]};
         u64 A[4] = {Bv[0], Bv[1], Bv[2], Bv[3]};
@@ -234,15 +316,19 @@ __device__ __forceinline__ void pass_tile_p(u64* sm, const u64* in, u64* out, u6
           A[3] = A1.y;
         }
         u64 o[4];
-        pointwise4<PR>(o, A, Bv, __ldg(twv + ((base + g4) >> 2)));
+        pointwise4<PR>(o, A, Bv, twsv[deep + (g4 >> 2)]);
 #pragma unroll
         for (int q = 0; q < 4; ++q) sm[pad16(g4 + q)] = o[q];
       }
       __syncthreads();
-      tile_inverse<C, PR>(sm, R, ksb, itab + (u64)PR * tab_stride);
+      const u64* itw = itab + (u64)PR * tab_stride;
+      stage_twiddles(tws, itw, ksb, R);
+      cp_async_wait_all();
+      __syncthreads();
+      tile_inverse<C, PR>(sm, R, ksb, itw, tws);
     }
   } else {
-    tile_inverse<C, PR>(sm, R, ksb, tw);
+    tile_inverse<C, PR>(sm, R, ksb, tw, tws);
   }
 
   u64* dst = out + (u64)PR * L;
@@ -250,8 +336,8 @@ __device__ __forceinline__ void pass_tile_p(u64* sm, const u64* in, u64* out, u6
     const u64 pos = base + ((u64)(idx >> LGC) << lg_s) + (idx & (C - 1));
     ulonglong2 v = make_ulonglong2(sm[pad16(idx)], sm[pad16(idx + 1)]);
     if (SCALE) {
-      v.x = div_pow2(v.x, (u32)(s - 1), p);
-      v.y = div_pow2(v.y, (u32)(s - 1), p);
+      v.x = div_pow2(canon_c<PR>(v.x), (u32)(s - 1), p);
+      v.y = div_pow2(canon_c<PR>(v.y), (u32)(s - 1), p);
     }
     st2<CG>(dst + pos, v);
   }

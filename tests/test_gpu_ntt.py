@@ -19,9 +19,11 @@ def ctx():
 
 @pytest.mark.parametrize("s,n", [(3, 2), (3, 4), (4, 7), (10, 300), (10, 1000), (12, 2048), (12, 3000),
                                  (14, 16384), (15, 9000), (21, 1 << 20), (21, (1 << 20) + 12345), (23, 3 << 21)])
-def test_forward_residues_bit_identical(ctx, oracle, s, n):
-    """Residues after load + forward NTT equal the oracle's raw values exactly
-    (same CRT-tree order, same lazy [0,2p) representation)."""
+def test_forward_residues_canonical(ctx, oracle, s, n):
+    """Residues after load + forward NTT equal the oracle's (the reference's
+    transform: same CRT-tree order and twiddles) modulo each prime, and stay in
+    the lazy ranges the next stage accepts: [0, 4p) for p0 and p1 (4p < 2^64),
+    [0, 2p) for p2."""
     a = limbs(1000 + s * 7 + n, n)
     t = ctx.transform().forward(to_dev(a), s)
     out = empty_dev(3 << s)
@@ -29,8 +31,10 @@ def test_forward_residues_bit_identical(ctx, oracle, s, n):
     got = to_host(out).reshape(3, 1 << s)
     want = oracle.ntt_forward(a, s)
     for i in range(3):
-        if not np.array_equal(got[i], want[i]):
-            bad = np.nonzero(got[i] != want[i])[0]
+        p = np.uint64(P[i])
+        assert int(got[i].max()) < (4 if i < 2 else 2) * P[i]
+        if not np.array_equal(got[i] % p, want[i] % p):
+            bad = np.nonzero(got[i] % p != want[i] % p)[0]
             pytest.fail(f"prime {i}: {bad.size} mismatches, first at {bad[:5]}")
 
 
@@ -41,7 +45,6 @@ def test_forward_golden_canonical(ctx, golden):
         out = empty_dev(3 << s)
         t.residues(out)
         got = to_host(out).reshape(3, 1 << s)
-        assert digest(got.ravel()) == c["raw"]
         canon = np.stack([got[i] % np.uint64(P[i]) for i in range(3)])
         assert digest(canon.ravel()) == c["canonical"]
 
