@@ -28,7 +28,7 @@ namespace {
 // Per-call scan: tile ids come from an atomic counter, so every predecessor
 // of a tile has started before it.
 template <class Prod>
-__global__ void __launch_bounds__(kScanThreads) scan_kernel(Prod prod, u64 total, u64* out, u64 out_limit,
+__global__ void __launch_bounds__(kScanThreads, 3) scan_kernel(Prod prod, u64 total, u64* out, u64 out_limit,
                                                             u64* side, u32* flags, u32* counter, u32* err) {
   __shared__ u32 s_tile;
   if (threadIdx.x == 0) s_tile = atomicAdd(counter, 1u);

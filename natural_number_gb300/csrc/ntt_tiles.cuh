@@ -206,12 +206,12 @@ __device__ __forceinline__ void run_group(u64* sm, int k, int l, int R, u64 ksb,
     level_group<1, C, INV, PR>(sm, l, R, ksb, tw, tws);
 }
 
-// Forward levels [0, R) of the tile in shared memory.
+// Forward levels [l0, R) of the tile in shared memory.
 template <int C, int PR>
-__device__ __forceinline__ void tile_forward(u64* sm, int R, u64 ksb, const u64* tw, const u64* tws) {
+__device__ __forceinline__ void tile_forward(u64* sm, int R, u64 ksb, const u64* tw, const u64* tws, int l0 = 0) {
   const int cap = group_cap(C, R);
-  const int n = (R + cap - 1) / cap;
-  for (int g = 0, l = 0; g < n; ++g) {
+  const int n = (R - l0 + cap - 1) / cap;
+  for (int g = 0, l = l0; g < n; ++g) {
     const int k = (R - l + (n - g) - 1) / (n - g);
     run_group<C, false, PR>(sm, k, l, R, ksb, tw, tws);
     __syncthreads();
@@ -271,9 +271,14 @@ __device__ __forceinline__ void pass_tile_p(u64* sm, const u64* in, u64* out, u6
   const u32 nel = (u32)C << R;
   constexpr int LGC = C == 16 ? 4 : 1;
 
+  // With every limb in the lower half of the transform (n_in <= L/2), level 0
+  // pairs each limb with a zero: both outputs are the limb's residue, written
+  // at once, and the tile starts at level 1.
+  const bool half = FIRST && lambda0 == 0 && n_in <= (L >> 1);
   if (FIRST) {
     const bool vec = ((reinterpret_cast<unsigned long long>(in) & 15) == 0);
-    for (u32 idx = 2 * threadIdx.x; idx < nel; idx += 2 * blockDim.x) {
+    const u32 nload = half ? nel / 2 : nel;
+    for (u32 idx = 2 * threadIdx.x; idx < nload; idx += 2 * blockDim.x) {
       const u64 pos = base + ((u64)(idx >> LGC) << lg_s) + (idx & (C - 1));
       u64 x0 = 0, x1 = 0;
       if (vec && pos + 1 < n_in) {
@@ -284,8 +289,14 @@ __device__ __forceinline__ void pass_tile_p(u64* sm, const u64* in, u64* out, u6
         if (pos < n_in) x0 = in[pos];
         if (pos + 1 < n_in) x1 = in[pos + 1];
       }
-      sm[pad16(idx)] = pos < n_in ? limb_mod(x0, PrimeC<PR>::m64, p, ch) : 0;
-      sm[pad16(idx + 1)] = pos + 1 < n_in ? limb_mod(x1, PrimeC<PR>::m64, p, ch) : 0;
+      const u64 r0 = pos < n_in ? limb_mod(x0, PrimeC<PR>::m64, p, ch) : 0;
+      const u64 r1 = pos + 1 < n_in ? limb_mod(x1, PrimeC<PR>::m64, p, ch) : 0;
+      sm[pad16(idx)] = r0;
+      sm[pad16(idx + 1)] = r1;
+      if (half) {
+        sm[pad16(idx + nload)] = r0;
+        sm[pad16(idx + nload + 1)] = r1;
+      }
     }
   } else {
     const u64* src = in + (u64)PR * L;
@@ -300,7 +311,7 @@ __device__ __forceinline__ void pass_tile_p(u64* sm, const u64* in, u64* out, u6
   __syncthreads();
 
   if (!INV) {
-    tile_forward<C, PR>(sm, R, ksb, tw, tws);
+    tile_forward<C, PR>(sm, R, ksb, tw, tws, half ? 1 : 0);
     if (FUSED) {  // contiguous tile: smem index == position - base; other == nullptr squares
       const u64* oth = other ? other + (u64)PR * L : nullptr;
       const ulonglong2* twsv = reinterpret_cast<const ulonglong2*>(tws);

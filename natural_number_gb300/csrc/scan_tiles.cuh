@@ -191,11 +191,23 @@ __device__ __forceinline__ void scan_tile(const Prod& prod, u64 tile, u64 total,
   }
   s_h0[tid] = c0;
   s_h1[tid] = c1;
+  // Overflow of the E positions before this tile: lanes 0..E-1 of warp 0
+  // produce one value each, thread 0 chains them.
+  __shared__ u64 s_x[E][3];
+  if (warp == 0) {
+    if (lane < E && tile != 0) {
+      const W3 x = prod(tile * kScanTile - E + lane);
+      s_x[lane][0] = x.w0;
+      s_x[lane][1] = x.w1;
+      s_x[lane][2] = x.w2;
+    }
+    __syncwarp();
+  }
   u64 hp0 = 0, hp1 = 0;
-  if (tid == 0 && k0 != 0) {  // overflow of the E positions before this tile
+  if (tid == 0 && tile != 0) {
     u64 d0 = 0, d1 = 0;
     for (int e = 0; e < E; ++e) {
-      W3 x = prod(k0 - E + e);
+      const W3 x{s_x[e][0], s_x[e][1], s_x[e][2]};
       const u64 s0 = x.w0 + d0;
       const u64 cy0 = s0 < d0;
       u64 s1 = x.w1 + d1;
