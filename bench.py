@@ -298,7 +298,7 @@ def main() -> None:
     ap.add_argument("--no-batch", action="store_true", help="skip the uneven-size batch measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the served request stream")
     ap.add_argument("--serve-jobs", type=int, default=300)
-    ap.add_argument("--series", action="store_true", help="also time pi and e to 10^8 digits (about a minute)")
+    ap.add_argument("--no-series", action="store_true", help="skip pi and e to 10^8 digits (a few seconds)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -387,7 +387,7 @@ def main() -> None:
         from natural_number_gb300 import serving as serving_mod
         serving = serving_mod.measure(args.serve_jobs)
 
-    series = measure_series(ctx) if args.series and rank == 0 else None
+    series = measure_series(ctx) if not args.no_series and rank == 0 else None
 
     if rank != 0:
         return
