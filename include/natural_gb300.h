@@ -77,7 +77,9 @@ nn_status nn_transform_pointwise(nn_context* ctx, nn_transform* dst, const nn_tr
  * residues are consumed.  *written (host) receives the limb count written. */
 nn_status nn_transform_inverse_save(nn_context* ctx, nn_transform* t, uint64_t* d_out, uint64_t size,
                                     uint64_t* written);
-/* Copies the 3 x 2^scale residues (prime-major) to d_out (inspection/testing). */
+/* Copies the 3 x 2^scale residues (prime-major) to d_out (inspection/testing):
+ * the reference's transform modulo each prime, as lazy representatives in
+ * [0, 4p) for p0 and p1 and [0, 2p) for p2. */
 nn_status nn_transform_residues(nn_context* ctx, const nn_transform* t, uint64_t* d_out);
 
 /* ---- products on device pointers ---------------------------------------- */

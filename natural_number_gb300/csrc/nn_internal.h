@@ -84,8 +84,9 @@ cudaError_t batch_configure(int* blocks_per_sm, size_t smem);
 cudaError_t batch_launch(const BatchJob* jobs, const BatchItem* items, u32 n_items, const u32* need, u32* done,
                          u32* head, u32* flags, u32* err, const Tables& t, int grid, size_t smem, cudaStream_t st);
 
-// Forward transform: limbs (n <= 2^s) -> residues [3][2^s], raw values in
-// [0,2p) identical to NTT_info::load + NTT (ntt_info.h:147-198).
+// Forward transform: limbs (n <= 2^s) -> residues [3][2^s] equal to
+// NTT_info::load + NTT (ntt_info.h:147-198) modulo each prime; lazy values in
+// [0, 4p) for p0 and p1, [0, 2p) for p2.
 cudaError_t ntt_forward(const u64* limbs, u64 n, u64* res, int s, const Tables& t, cudaStream_t st,
                         const std::vector<Pass>* plan = nullptr);
 // Pointwise product of degree-1 residues (ntt_info.h:224-231); dst may alias a or b.

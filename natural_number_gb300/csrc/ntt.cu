@@ -5,17 +5,19 @@
 // level lambda (0 <= lambda <= s-2) splits each block of 2^(s-lambda) words into
 // halves x, y and applies (x, y) -> (x + w y, x - w y) with w = root[2b] for
 // block b.  Level 0 is the load's radix-2 stage (ntt_info.h:153-171, twiddle
-// 1); the last level (pairs) is folded into the pointwise product.  Because
-// every butterfly reduces exactly, the residues after each level are
-// bit-identical to the reference's, whatever the grouping of levels.
+// 1); the last level (pairs) is folded into the pointwise product.  The
+// residues after each level equal the reference's modulo each prime, whatever
+// the grouping of levels; only their lazy representatives differ for p0 and
+// p1 (values kept in [0, 4p), see ntt_tiles.cuh).
 //
 // GPU mapping: levels are grouped into passes.  A pass over levels
 // [lambda0, lambda0+R) sees, inside each block of 2^(s-lambda0) words, S = 2^(s-
 // lambda0-R) interleaved columns of 2^R rows (row stride S).  A CTA stages
 // C columns x 2^R rows of one prime in shared memory with coalesced row
 // segments, runs the R levels as radix-8/4/2 register units (twiddles read
-// as 16-byte (w, w') pairs through the read-only cache), and writes the tile
-// back.  The first forward pass reads limbs and reduces them on the fly; the
+// as 16-byte (w, w') pairs: through the read-only cache in the strided
+// passes, staged in shared memory with the tile in the contiguous ones), and
+// writes the tile back.  The first forward pass reads limbs and reduces them on the fly; the
 // last inverse pass applies the 2^-(s-1) scale on the way out.
 #include <cuda_runtime.h>
 
