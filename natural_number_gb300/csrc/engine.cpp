@@ -27,6 +27,10 @@ struct nn_context {
   int device = 0;
   cudaStream_t own = nullptr;
   cudaStream_t stream = nullptr;
+  // host-pointer calls: the second operand's copy runs on `copy` while the
+  // first operand is transformed
+  cudaStream_t copy = nullptr;
+  cudaEvent_t ev_first = nullptr, ev_second = nullptr;
   u64 budget = 0;
   u64 held = 0;  // bytes of live allocations made through the context
   nn::Tables tables;
@@ -191,10 +195,16 @@ nn_status forward_fused(nn_context* c, nn_transform* t, const u64* d_limbs, u64 
 }
 
 // Balanced NTT product at scale s into d_out (size limbs, or wrap).
+// b_ready (optional): an event b's contents wait for; the stream waits for it
+// only after a's forward transform.
 nn_status ntt_product(nn_context* c, u64* d_out, const u64* a, u64 na, const u64* b, u64 nb, int s, u64 size,
-                      u64* written) {
+                      u64* written, cudaEvent_t b_ready = nullptr) {
   nn_transform xa, xb;
   nn_status st = forward(c, &xa, a, na, s);
+  if (st == NN_OK && b_ready) {
+    const cudaError_t e = cudaStreamWaitEvent(c->stream, b_ready, 0);
+    if (e != cudaSuccess) st = fail(c, e, "wait for the second operand");
+  }
   if (st == NN_OK && c->passes(s).size() >= 2) {
     st = forward_fused(c, &xb, b, nb, s, &xa);
     if (st == NN_OK) st = inverse_save(c, &xb, d_out, size, written, true);
@@ -208,7 +218,10 @@ nn_status ntt_product(nn_context* c, u64* d_out, const u64* a, u64 na, const u64
   return st;
 }
 
-nn_status mul_impl(nn_context* c, u64* d_out, const u64* a, u64 na, const u64* b, u64 nb) {
+// b_ready (optional): an event the contents of b wait for; the balanced NTT
+// product waits for it after a's forward transform, the other paths at once.
+nn_status mul_impl(nn_context* c, u64* d_out, const u64* a, u64 na, const u64* b, u64 nb,
+                   cudaEvent_t b_ready = nullptr) {
   if (!d_out || !a || !b || na == 0 || nb == 0) {
     c->err = "mul: null pointer or empty operand";
     return NN_ERR_INVALID;
@@ -216,15 +229,22 @@ nn_status mul_impl(nn_context* c, u64* d_out, const u64* a, u64 na, const u64* b
   if (na < nb) {
     std::swap(a, b);
     std::swap(na, nb);
+    if (b_ready) NN_CK(c, cudaStreamWaitEvent(c->stream, b_ready, 0), "wait for an operand");
+    b_ready = nullptr;
+  }
+  const u64 a0 = (na + 1) >> 1;
+  const bool balanced = nb >= kNttMulThreshold && ntt_scale(na, nb) == ntt_scale(a0, nb);
+  if (b_ready && !balanced) {
+    NN_CK(c, cudaStreamWaitEvent(c->stream, b_ready, 0), "wait for an operand");
+    b_ready = nullptr;
   }
   if (nb < kNttMulThreshold) {  // natural.h:445-446 -> _mul_base
     NN_CK(c, nn::school_mul(a, na, b, nb, d_out, c->scan, c->stream), "base-case product");
     return NN_OK;
   }
   // natural::_mul_NTT (natural.h:391-419)
-  const u64 a0 = (na + 1) >> 1;
   const int s = ntt_scale(na, nb), s_opt = ntt_scale(a0, nb);
-  if (s == s_opt) return ntt_product(c, d_out, a, na, b, nb, s, na + nb, nullptr);
+  if (s == s_opt) return ntt_product(c, d_out, a, na, b, nb, s, na + nb, nullptr, b_ready);
   // Unbalanced: b's transform is made once at s_opt and reused for both
   // halves of a (mul_save_NTT_info / mul_load_NTT_info, natural.h:452-515).
   const u64 a1 = na - a0;
@@ -508,6 +528,9 @@ nn_status nn_context_create(int device, uint64_t budget, nn_context** out) {
   c->budget = budget;
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_first, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_second, cudaEventDisableTiming);
   if (e == cudaSuccess) e = nn::upload_primes();
   if (e == cudaSuccess) {
     cudaMemPool_t pool;
@@ -521,6 +544,9 @@ nn_status nn_context_create(int device, uint64_t budget, nn_context** out) {
   if (e != cudaSuccess) {
     nn_status st = e == cudaErrorNoDevice || e == cudaErrorNoKernelImageForDevice ? NN_ERR_NO_DEVICE : NN_ERR_CUDA;
     cudaGetLastError();
+    if (c->ev_second) cudaEventDestroy(c->ev_second);
+    if (c->ev_first) cudaEventDestroy(c->ev_first);
+    if (c->copy) cudaStreamDestroy(c->copy);
     if (c->own) cudaStreamDestroy(c->own);
     delete c;
     return st;
@@ -542,6 +568,10 @@ nn_status nn_context_destroy(nn_context* c) {
   cudaStreamSynchronize(c->own);
   nn::tables_free(c->tables);
   nn::scan_free(c->scan);
+  cudaStreamSynchronize(c->copy);
+  cudaEventDestroy(c->ev_second);
+  cudaEventDestroy(c->ev_first);
+  cudaStreamDestroy(c->copy);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
   return NN_OK;
@@ -654,15 +684,27 @@ nn_status nn_mul_base(nn_context* c, uint64_t* d_out, const uint64_t* a, uint64_
 nn_status nn_mul_host(nn_context* c, uint64_t* out, uint64_t* out_n, const uint64_t* a, uint64_t na,
                       const uint64_t* b, uint64_t nb) {
   if (!c || !out || !a || !b || !na || !nb) return NN_ERR_INVALID;
+  if (na < nb) {  // the longer operand first: it is transformed first
+    std::swap(a, b);
+    std::swap(na, nb);
+  }
   u64 *da, *db, *dout;
   nn_status st = scratch(c, 0, na, &da);
   if (st == NN_OK) st = scratch(c, 1, nb, &db);
   if (st == NN_OK) st = scratch(c, 2, na + nb, &dout);
   if (st != NN_OK) return st;
+  // a on the context's stream; b on the copy stream once a is in, so that
+  // b's copy runs while a is transformed.
   NN_CK(c, cudaMemcpyAsync(da, a, na * 8, cudaMemcpyHostToDevice, c->stream), "H2D");
-  NN_CK(c, cudaMemcpyAsync(db, b, nb * 8, cudaMemcpyHostToDevice, c->stream), "H2D");
-  st = mul_impl(c, dout, da, na, db, nb);
-  if (st != NN_OK) return st;
+  NN_CK(c, cudaEventRecord(c->ev_first, c->stream), "event record");
+  NN_CK(c, cudaStreamWaitEvent(c->copy, c->ev_first, 0), "copy stream wait");
+  NN_CK(c, cudaMemcpyAsync(db, b, nb * 8, cudaMemcpyHostToDevice, c->copy), "H2D");
+  NN_CK(c, cudaEventRecord(c->ev_second, c->copy), "event record");
+  st = mul_impl(c, dout, da, na, db, nb, c->ev_second);
+  if (st != NN_OK) {
+    cudaStreamSynchronize(c->copy);
+    return st;
+  }
   NN_CK(c, cudaMemcpyAsync(out, dout, (na + nb) * 8, cudaMemcpyDeviceToHost, c->stream), "D2H");
   st = nn_context_synchronize(c);
   if (st == NN_OK && out_n) *out_n = normalized(out, na + nb);
