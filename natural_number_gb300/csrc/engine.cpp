@@ -688,6 +688,9 @@ nn_status nn_mul_host(nn_context* c, uint64_t* out, uint64_t* out_n, const uint6
     std::swap(a, b);
     std::swap(na, nb);
   }
+  // Copies, not kernels reading and writing page-locked host memory in
+  // place: measured on GB300 at 2^27 limbs, in-place access over the host
+  // link made the product 7 to 95 ms slower than these copies.
   u64 *da, *db, *dout;
   nn_status st = scratch(c, 0, na, &da);
   if (st == NN_OK) st = scratch(c, 1, nb, &db);

@@ -96,11 +96,16 @@ __global__ void twiddle_extend_kernel(u64* tab, u64 n, u64 bw, u64 bwp, int prim
 
 // FIRST: input is limbs (n_in of them, zero beyond); otherwise residues [3][L].
 // SCALE: multiply by 2^-(s-1) on the way out (last inverse pass).
+// The first pass numbers its CTAs prime-fastest (x = 3 * tile + prime): the
+// three CTAs that reduce the same limbs run together, so the limbs cross HBM
+// about once and reach the other two through L2.
 template <int C, bool FIRST, bool INV, bool SCALE>
 __global__ void __launch_bounds__(256, 4) ntt_pass_kernel(const u64* in, u64* out, u64 n_in, int s, int lambda0, int R,
                                                        const u64* __restrict__ tab, u64 tab_stride) {
   extern __shared__ u64 sm[];
-  pass_tile<C, FIRST, INV, SCALE, false>(sm, in, out, n_in, s, lambda0, R, tab, tab_stride, blockIdx.y, blockIdx.x);
+  const int prime = FIRST ? (int)(blockIdx.x % 3) : (int)blockIdx.y;
+  const u64 tile = FIRST ? blockIdx.x / 3 : blockIdx.x;
+  pass_tile<C, FIRST, INV, SCALE, false>(sm, in, out, n_in, s, lambda0, R, tab, tab_stride, prime, tile);
 }
 
 // Contiguous last pass: forward levels, pointwise by `other` (nullptr
@@ -131,7 +136,7 @@ cudaError_t launch_pass(const u64* in, u64* out, u64 n_in, int s, const Pass& ps
     configured = true;
   }
   const u64 tiles = (1ull << s) / ((u64)ps.C << ps.R);
-  dim3 grid((unsigned)tiles, 3);
+  const dim3 grid = FIRST ? dim3((unsigned)(3 * tiles), 1) : dim3((unsigned)tiles, 3);
   const char* name = C == 2 ? (INV ? "ntt_inv_row_pass" : "ntt_fwd_row_pass")
                             : FIRST ? "ntt_fwd_load_col_pass"
                                     : INV ? (SCALE ? "ntt_inv_last_col_pass" : "ntt_inv_col_pass") : "ntt_fwd_col_pass";

@@ -151,3 +151,21 @@ def test_config2_large_multiply_and_square(ctx, golden):
     for c in golden.get("big_sqr", []):
         if c["n"] == n:
             assert digest(normalize(sq)) == c["out"]
+
+
+@pytest.mark.parametrize("na,nb", [(1 << 16, 1 << 16), (50000, 3000), (200, 150), (70000, 65536)])
+def test_mul_host_page_locked(ctx, oracle, na, nb):
+    """Host products on page-locked operands and result (as the benchmark's
+    end-to-end leg uses them), for the balanced NTT, split and base-case
+    paths, in both operand orders; and the same product from pageable arrays."""
+    import torch
+    a, b = limbs(31 + na, na), limbs(37 + nb, nb)
+    pa = torch.from_numpy(a).pin_memory().numpy()
+    pb = torch.from_numpy(b).pin_memory().numpy()
+    po = torch.zeros(na + nb, dtype=torch.uint64).pin_memory().numpy()
+    want = oracle.mul(a, b)
+    got = ctx.mul(pa, pb, out=po)
+    assert np.array_equal(got, want)
+    got = ctx.mul(pb, pa, out=po)  # shorter operand first
+    assert np.array_equal(got, want)
+    assert np.array_equal(ctx.mul(a, b), want)  # pageable
