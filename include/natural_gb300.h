@@ -217,6 +217,13 @@ nn_status nn_sqr_host(nn_context* ctx, uint64_t* out, uint64_t* out_n, const uin
  * as the reference's natural holds them (natural::std normalisation where it
  * applies). */
 void nn_free(void* p);
+/* Page-locked host memory for limb buffers (the drop-in natural's buffers of
+ * 64 KiB and more): copies between such buffers and the GPU run at the host
+ * link's speed.  Blocks are recycled by size; nn_host_alloc falls back to
+ * malloc when no page-locked memory can be had, and nn_host_free takes either
+ * kind (bytes = the size passed to nn_host_alloc).  Thread-safe. */
+void* nn_host_alloc(uint64_t bytes);
+void nn_host_free(void* p, uint64_t bytes);
 /* natural::_div (natural.h:749-769): quotient and remainder. */
 nn_status nn_div_host(nn_context* ctx, const uint64_t* a, uint64_t n_a, const uint64_t* b, uint64_t n_b,
                       uint64_t** q, uint64_t* q_n, uint64_t** r, uint64_t* r_n);

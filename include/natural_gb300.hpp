@@ -148,28 +148,44 @@ constexpr int NTTscale_threshold = 10;      // ntt_info.h:8
 }  // namespace nn_gb300
 
 // ---------------------------------------------------------------------------
-// basic_natural (basic_natural.h:9-97): malloc'd limbs, capacity = bit_ceil.
+// basic_natural (basic_natural.h:9-97): limbs with capacity = bit_ceil(size).
+// Buffers of 64 KiB and more come from the library's page-locked host pool,
+// so the copies to and from the GPU around every product run at the host
+// link's speed; smaller ones are malloc'd as in the reference.  Which
+// allocator a buffer came from follows from its capacity alone.
 // ---------------------------------------------------------------------------
+namespace nn_gb300 {
+constexpr uint64_t kPinnedLimbs = 1u << 13;
+inline uint64_t* limb_alloc(uint64_t cap) {
+  void* p = cap >= kPinnedLimbs ? nn_host_alloc(cap * 8) : std::malloc(cap * 8);
+  if (!p) throw std::bad_alloc();
+  return static_cast<uint64_t*>(p);
+}
+inline void limb_free(uint64_t* p, uint64_t cap) {
+  if (!p) return;
+  if (cap >= kPinnedLimbs)
+    nn_host_free(p, cap * 8);
+  else
+    std::free(p);
+}
+}  // namespace nn_gb300
+
 struct basic_natural {
   uint64_t* data;
   uint64_t size;
   uint64_t capacity;
 
-  basic_natural() : data((uint64_t*)std::malloc(8)), size(1), capacity(1) {
-    if (!data) throw std::bad_alloc();
-  }
+  basic_natural() : data(nn_gb300::limb_alloc(1)), size(1), capacity(1) {}
   basic_natural(std::initializer_list<uint64_t> n) : size(n.size()), capacity(std::bit_ceil(n.size())) {
-    data = (uint64_t*)std::malloc(capacity * 8);
-    if (!data) throw std::bad_alloc();
+    data = nn_gb300::limb_alloc(capacity);
     std::memcpy(data, n.begin(), size * 8);
   }
   basic_natural(const basic_natural& n) : size(n.size), capacity(std::bit_ceil(n.size)) {
-    data = (uint64_t*)std::malloc(capacity * 8);
-    if (!data) throw std::bad_alloc();
+    data = nn_gb300::limb_alloc(capacity);
     std::memcpy(data, n.data, size * 8);
   }
   basic_natural(basic_natural&& n) noexcept : data(n.data), size(n.size), capacity(n.capacity) { n.data = nullptr; }
-  ~basic_natural() { std::free(data); }
+  ~basic_natural() { nn_gb300::limb_free(data, capacity); }
   basic_natural& operator=(const basic_natural& n) {
     if (this != &n) {
       resize(n.size);
@@ -179,7 +195,7 @@ struct basic_natural {
   }
   basic_natural& operator=(basic_natural&& n) noexcept {
     if (this != &n) {
-      std::free(data);
+      nn_gb300::limb_free(data, capacity);
       data = n.data;
       size = n.size;
       capacity = n.capacity;
@@ -190,10 +206,12 @@ struct basic_natural {
   void resize(uint64_t s) {
     size = s;
     if (capacity < s) {
-      capacity = std::bit_ceil(s);
-      uint64_t* p = (uint64_t*)std::realloc(data, capacity * 8);
-      if (!p) throw std::bad_alloc();
+      const uint64_t cap = std::bit_ceil(s);
+      uint64_t* p = nn_gb300::limb_alloc(cap);
+      if (data) std::memcpy(p, data, capacity * 8);  // what realloc would keep
+      nn_gb300::limb_free(data, capacity);
       data = p;
+      capacity = cap;
     }
   }
   uint64_t& operator[](uint64_t i) { return data[i]; }

@@ -6,8 +6,13 @@
 
 #include <algorithm>
 #include <bit>
+#include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
+#include <unordered_map>
+#include <unordered_set>
+#include <vector>
 
 #include "../../include/natural_gb300.h"
 #include "nn_internal.h"
@@ -486,7 +491,56 @@ u64 normalized(const u64* x, u64 n) {  // natural::std (natural.h:82-93)
 
 }  // namespace
 
+// Page-locked host blocks for limb buffers, recycled by size (cudaMallocHost
+// pins pages and is far too slow to call per buffer).  Intentionally never
+// destroyed: blocks may be freed during static destruction.
+struct HostPool {
+  std::mutex mu;
+  std::unordered_map<u64, std::vector<void*>> free_blocks;  // bytes -> blocks
+  std::unordered_set<void*> pinned;
+};
+HostPool& host_pool() {
+  static HostPool* p = new HostPool;
+  return *p;
+}
+
 extern "C" {
+
+void* nn_host_alloc(uint64_t bytes) {
+  if (bytes == 0) bytes = 8;
+  HostPool& P = host_pool();
+  {
+    std::lock_guard<std::mutex> g(P.mu);
+    auto it = P.free_blocks.find(bytes);
+    if (it != P.free_blocks.end() && !it->second.empty()) {
+      void* p = it->second.back();
+      it->second.pop_back();
+      return p;
+    }
+  }
+  void* p = nullptr;
+  if (cudaMallocHost(&p, bytes) == cudaSuccess && p) {
+    std::lock_guard<std::mutex> g(P.mu);
+    P.pinned.insert(p);
+    return p;
+  }
+  cudaGetLastError();
+  return std::malloc(bytes);
+}
+
+void nn_host_free(void* p, uint64_t bytes) {
+  if (!p) return;
+  if (bytes == 0) bytes = 8;
+  HostPool& P = host_pool();
+  {
+    std::lock_guard<std::mutex> g(P.mu);
+    if (P.pinned.count(p)) {
+      P.free_blocks[bytes].push_back(p);
+      return;
+    }
+  }
+  std::free(p);
+}
 
 const char* nn_status_string(nn_status s) {
   switch (s) {
