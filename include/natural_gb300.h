@@ -224,6 +224,18 @@ void nn_free(void* p);
  * kind (bytes = the size passed to nn_host_alloc).  Thread-safe. */
 void* nn_host_alloc(uint64_t bytes);
 void nn_host_free(void* p, uint64_t bytes);
+/* Host limb arithmetic for long operands, run on all host cores with the
+ * results of the sequential loops (asmAdd0/asmSub0/asmShl/asmShr, asm.h:7-33):
+ * the drop-in natural's O(n) steps between GPU products.  add/sub return the
+ * carry/borrow out, and d may be a or b.  shl writes n + 1 limbs and shr n,
+ * 1 <= cl <= 63; d may be s, or overlap it the way an in-place shift by whole
+ * limbs does (d above s for shl, below for shr), which then runs in sequence.
+ * copy is memmove. */
+int nn_host_add_n(uint64_t n, uint64_t* d, const uint64_t* a, const uint64_t* b);
+int nn_host_sub_n(uint64_t n, uint64_t* d, const uint64_t* a, const uint64_t* b);
+void nn_host_shl_n(unsigned cl, uint64_t n, const uint64_t* s, uint64_t* d);
+void nn_host_shr_n(unsigned cl, uint64_t n, const uint64_t* s, uint64_t* d);
+void nn_host_copy(uint64_t* d, const uint64_t* s, uint64_t n);
 /* natural::_div (natural.h:749-769): quotient and remainder. */
 nn_status nn_div_host(nn_context* ctx, const uint64_t* a, uint64_t n_a, const uint64_t* b, uint64_t n_b,
                       uint64_t** q, uint64_t* q_n, uint64_t** r, uint64_t* r_n);

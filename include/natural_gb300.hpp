@@ -62,7 +62,17 @@ inline void check(nn_status st, const char* what) {
 }
 
 // ---- host limb glue (the carry/borrow chains of asm.h:7-30) ---------------
+// From 2^16 limbs up these run on all host cores in the library
+// (nn_host_add_n and friends), with the same results.
+constexpr uint64_t kParallelLimbs = 1u << 16;
+inline void copy_n(uint64_t* d, const uint64_t* s, uint64_t n) {
+  if (n >= kParallelLimbs)
+    nn_host_copy(d, s, n);
+  else
+    std::memmove(d, s, n * 8);
+}
 inline int add_n(uint64_t n, uint64_t* d, const uint64_t* a, const uint64_t* b) {
+  if (n >= kParallelLimbs) return nn_host_add_n(n, d, a, b);
   uint64_t c = 0;
   for (uint64_t i = 0; i < n; ++i) {
     uint64_t s = a[i] + c;
@@ -79,10 +89,11 @@ inline int add_1(uint64_t n, const uint64_t* s, uint64_t* d, int cf) {
     d[i] = s[i] + 1;
     cf = d[i] == 0;
   }
-  if (i < n && d != s) std::memmove(d + i, s + i, (n - i) * 8);
+  if (i < n && d != s) copy_n(d + i, s + i, n - i);
   return cf;
 }
 inline int sub_n(uint64_t n, uint64_t* d, const uint64_t* a, const uint64_t* b) {
+  if (n >= kParallelLimbs) return nn_host_sub_n(n, d, a, b);
   uint64_t br = 0;
   for (uint64_t i = 0; i < n; ++i) {
     uint64_t x = a[i], y = b[i];
@@ -100,7 +111,7 @@ inline int sub_1(uint64_t n, const uint64_t* s, uint64_t* d, int cf) {
     d[i] = v - 1;
     cf = v == 0;
   }
-  if (i < n && d != s) std::memmove(d + i, s + i, (n - i) * 8);
+  if (i < n && d != s) copy_n(d + i, s + i, n - i);
   return cf;
 }
 // base.h:7-16
@@ -111,6 +122,7 @@ inline int sub(uint64_t* d, const uint64_t* a, uint64_t n1, const uint64_t* b, u
   return sub_1(n1 - n2, a + n2, d + n2, sub_n(n2, d, a, b));
 }
 inline void shl_n(unsigned cl, uint64_t n, const uint64_t* s, uint64_t* d) {  // asmShl semantics
+  if (n >= kParallelLimbs) return nn_host_shl_n(cl, n, s, d);
   uint64_t carry = 0;
   for (uint64_t i = n; i-- > 0;) {
     uint64_t x = s[i];
@@ -120,6 +132,7 @@ inline void shl_n(unsigned cl, uint64_t n, const uint64_t* s, uint64_t* d) {  //
   d[0] = carry << cl;
 }
 inline void shr_n(unsigned cl, uint64_t n, const uint64_t* s, uint64_t* d) {  // asmShr semantics
+  if (n >= kParallelLimbs) return nn_host_shr_n(cl, n, s, d);
   uint64_t cur = s[0];
   for (uint64_t i = 0; i + 1 < n; ++i) {
     uint64_t nx = s[i + 1];
@@ -182,14 +195,14 @@ struct basic_natural {
   }
   basic_natural(const basic_natural& n) : size(n.size), capacity(std::bit_ceil(n.size)) {
     data = nn_gb300::limb_alloc(capacity);
-    std::memcpy(data, n.data, size * 8);
+    nn_gb300::copy_n(data, n.data, size);
   }
   basic_natural(basic_natural&& n) noexcept : data(n.data), size(n.size), capacity(n.capacity) { n.data = nullptr; }
   ~basic_natural() { nn_gb300::limb_free(data, capacity); }
   basic_natural& operator=(const basic_natural& n) {
     if (this != &n) {
       resize(n.size);
-      std::memcpy(data, n.data, size * 8);
+      nn_gb300::copy_n(data, n.data, size);
     }
     return *this;
   }
@@ -208,7 +221,7 @@ struct basic_natural {
     if (capacity < s) {
       const uint64_t cap = std::bit_ceil(s);
       uint64_t* p = nn_gb300::limb_alloc(cap);
-      if (data) std::memcpy(p, data, capacity * 8);  // what realloc would keep
+      if (data) nn_gb300::copy_n(p, data, capacity);  // what realloc would keep
       nn_gb300::limb_free(data, capacity);
       data = p;
       capacity = cap;
@@ -378,7 +391,7 @@ inline natural& natural::_shl(const natural* ap, uint64_t b) {  // natural.h:244
   b &= 63;
   if (b == 0) {
     resize(as + n);
-    std::memmove(data + n, ap->data, as * 8);
+    nn_gb300::copy_n(data + n, ap->data, as);
     std::memset(data, 0, n * 8);
     return *this;
   }
@@ -396,7 +409,7 @@ inline natural& natural::_shr(const natural* ap, uint64_t b) {  // natural.h:275
   b &= 63;
   resize(as - n);
   if (b == 0) {
-    std::memmove(data, ap->data + n, (as - n) * 8);
+    nn_gb300::copy_n(data, ap->data + n, as - n);
     return *this;
   }
   nn_gb300::shr_n((unsigned)b, as - n, ap->data + n, data);
