@@ -110,9 +110,13 @@ __global__ void __launch_bounds__(256, 4) ntt_pass_kernel(const u64* in, u64* ou
 
 // Contiguous last pass: forward levels, pointwise by `other` (nullptr
 // squares), inverse levels, in one visit of each tile.
-__global__ void __launch_bounds__(256, 3) ntt_fused_kernel(u64* res, const u64* other, int s, int lambda0, int R,
-                                                        const u64* __restrict__ tab, const u64* __restrict__ itab,
-                                                        u64 tab_stride) {
+// Two register budgets: with tiles of up to 2^10 rows (33 KiB of shared
+// memory with their twiddles) four CTAs fit an SM if each stays within 64
+// registers; larger tiles fit three, which may use 80.
+template <int BLOCKS>
+__global__ void __launch_bounds__(256, BLOCKS) ntt_fused_kernel(u64* res, const u64* other, int s, int lambda0, int R,
+                                                             const u64* __restrict__ tab,
+                                                             const u64* __restrict__ itab, u64 tab_stride) {
   extern __shared__ u64 sm[];
   pass_tile<2, false, false, false, false, true>(sm, res, res, 0, s, lambda0, R, tab, tab_stride, blockIdx.y,
                                                  blockIdx.x, itab, other);
@@ -277,14 +281,19 @@ cudaError_t ntt_fused_last(u64* res, const u64* other, int s, const Tables& t, c
   const size_t smem = tile_smem_bytes(ps.C, ps.R);
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(ntt_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaError_t e = cudaFuncSetAttribute(ntt_fused_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(ntt_fused_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (e != cudaSuccess) return e;
     configured = true;
   }
   const u64 tiles = (1ull << s) / ((u64)ps.C << ps.R);
   dim3 grid((unsigned)tiles, 3);
   launch_begin("ntt_fused_row_pass", st);
-  ntt_fused_kernel<<<grid, 256, smem, st>>>(res, other, s, ps.lambda0, ps.R, t.root, t.iroot, t.cap);
+  if (4 * smem <= 227 * 1024)
+    ntt_fused_kernel<4><<<grid, 256, smem, st>>>(res, other, s, ps.lambda0, ps.R, t.root, t.iroot, t.cap);
+  else
+    ntt_fused_kernel<3><<<grid, 256, smem, st>>>(res, other, s, ps.lambda0, ps.R, t.root, t.iroot, t.cap);
   launch_end(st);
   return cudaGetLastError();
 }
