@@ -149,3 +149,19 @@ def test_to_dec_levels_golden(ctx, golden):
     for c in golden["pow"]:
         p = ctx.pow(np.array([c["base"]], dtype=np.uint64), c["e"])
         assert sdig(ctx.to_dec_levels(p, host_below=4)) == c["dec"]
+
+
+@pytest.mark.parametrize("kind", ["pi", "e"])
+def test_levels_1e7_and_1e8_digits(ctx, golden, kind):
+    """pi and e to 10^7 and 10^8 digits (the reference's recipes with 2^20 /
+    2^23 and 2^21 / 2^24 terms) with the default split between host subtrees
+    and GPU levels: SHA-256 of the digit strings equal to the reference's."""
+    import hashlib
+    for c in (golden[kind][4], golden["big_" + kind][0]):
+        if kind == "pi":
+            s, _ = ctx.pi_dec_levels(c["terms"], c["acc"], c["digits"])
+        else:
+            s, _ = ctx.e_dec_levels(c["terms"], c["digits"])
+        assert len(s) == c["out"]["len"]
+        assert hashlib.sha256(s.encode()).hexdigest() == c["out"]["sha256"]
+        del s

@@ -169,3 +169,18 @@ def test_mul_host_page_locked(ctx, oracle, na, nb):
     got = ctx.mul(pb, pa, out=po)  # shorter operand first
     assert np.array_equal(got, want)
     assert np.array_equal(ctx.mul(a, b), want)  # pageable
+
+
+@pytest.mark.parametrize("na,nb", [(1 << 25, 1000), (1 << 25, 383), ((1 << 24) + 12345, (1 << 20) + 7),
+                                   (3 << 23, 1 << 23), ((1 << 26) - 1, (1 << 26) - 1)])
+def test_large_unbalanced_products_mod_checks(ctx, na, nb):
+    """Large products through every dispatch path (schoolbook below 384 limbs,
+    the reference's unbalanced split, balanced NTT just below a scale
+    boundary), checked by the product's residues mod 2^64 - 1 and 2^64 + 1."""
+    a, b = limbs(101 + na, na), limbs(103 + nb, nb)
+    out = empty_dev(na + nb)
+    ctx.mul_device(out, to_dev(a), to_dev(b))
+    prod = to_host(out)
+    ma, mb, mp = mod_checks(a), mod_checks(b), mod_checks(prod)
+    assert mp[0] == ma[0] * mb[0] % (2**64 - 1)
+    assert mp[1] == ma[1] * mb[1] % (2**64 + 1)
