@@ -52,7 +52,7 @@ __device__ __forceinline__ void run_pass(u64* sm, const BatchJob& J, const Batch
   }
 }
 
-__global__ void __launch_bounds__(256) batch_kernel(const BatchJob* __restrict__ jobs,
+__global__ void __launch_bounds__(256, 3) batch_kernel(const BatchJob* __restrict__ jobs,
                                                     const BatchItem* __restrict__ items, u32 n_items,
                                                     const u32* __restrict__ need, u32* done, u32* head, u32* flags,
                                                     u32* err, Tables t) {
