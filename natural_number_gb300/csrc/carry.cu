@@ -15,6 +15,9 @@
 // wait is bounded and records an error instead of hanging.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <functional>
+
 #include "nn_device.cuh"
 #include "nn_internal.h"
 #include "scan_tiles.cuh"
@@ -25,13 +28,15 @@ NN_DEFINE_PRIME_UPLOADER(upload_primes_carry)
 
 namespace {
 
-// Per-call scan: tile ids come from an atomic counter, so every predecessor
-// of a tile has started before it.
+// Per-call scan: tile ids come from an atomic counter (from tile_base), so
+// every predecessor of a tile has started before it, in this launch or in an
+// earlier one on the stream.
 template <class Prod>
 __global__ void __launch_bounds__(kScanThreads, 3) scan_kernel(Prod prod, u64 total, u64* out, u64 out_limit,
-                                                            u64* side, u32* flags, u32* counter, u32* err) {
+                                                            u64* side, u32* flags, u32* counter, u32* err,
+                                                            u32 tile_base) {
   __shared__ u32 s_tile;
-  if (threadIdx.x == 0) s_tile = atomicAdd(counter, 1u);
+  if (threadIdx.x == 0) s_tile = tile_base + atomicAdd(counter, 1u);
   __syncthreads();
   scan_tile(prod, s_tile, total, out, out_limit, side, flags, err);
 }
@@ -84,19 +89,25 @@ __global__ void wait_probe_kernel(const u32* flag, u32* err, int limit) {
   if (threadIdx.x == 0 && wait_flag(flag, limit) == 0) atomicExch(err, 1u);
 }
 
+// Tiles [tile_begin, tile_end) of the scan (all of them by default); the
+// status words are cleared with the first range, so the ranges of one scan
+// go in order on one stream.
 template <class Prod>
 cudaError_t run_scan(const Prod& prod, u64 total, u64* out, u64 out_limit, Scan& sc, cudaStream_t st,
-                     const char* name) {
+                     const char* name, u64 tile_begin = 0, u64 tile_end = ~0ull) {
   const u64 tiles = scan_tiles(total);
+  tile_end = std::min(tile_end, tiles);
   cudaError_t e = scan_reserve(sc, tiles);
   if (e != cudaSuccess) return e;
-  e = cudaMemsetAsync(sc.flags, 0, (tiles + 1) * sizeof(u32), st);
-  if (e != cudaSuccess) return e;
+  if (tile_begin == 0) {
+    e = cudaMemsetAsync(sc.flags, 0, (tiles + 1) * sizeof(u32), st);
+    if (e != cudaSuccess) return e;
+  }
   e = cudaMemsetAsync(sc.counter, 0, sizeof(u32), st);
   if (e != cudaSuccess) return e;
   launch_begin(name, st);
-  scan_kernel<Prod><<<(unsigned)tiles, kScanThreads, 0, st>>>(prod, total, out, out_limit, sc.side, sc.flags,
-                                                              sc.counter, sc.err);
+  scan_kernel<Prod><<<(unsigned)(tile_end - tile_begin), kScanThreads, 0, st>>>(
+      prod, total, out, out_limit, sc.side, sc.flags, sc.counter, sc.err, (u32)tile_begin);
   launch_end(st);
   return cudaGetLastError();
 }
@@ -148,6 +159,21 @@ cudaError_t ntt_save(const u64* res, int s, u64* out, u64 size, Scan& sc, u64* w
   }
   *written = size;
   return run_scan(CrtProducer{res, L, size - 1}, size, out, size, sc, st, "crt_carry_scan");
+}
+
+cudaError_t ntt_save_chunks(const u64* res, int s, u64* out, u64 size, Scan& sc, cudaStream_t st, int chunks,
+                            const std::function<cudaError_t(u64, u64)>& done) {
+  const u64 L = 1ull << s;
+  if (size - 1 > L || chunks < 1) return cudaErrorInvalidValue;  // normal mode only
+  const u64 tiles = scan_tiles(size);
+  cudaError_t e = scan_reserve(sc, tiles);
+  for (int k = 0; k < chunks && e == cudaSuccess; ++k) {
+    const u64 t0 = tiles * k / chunks, t1 = tiles * (k + 1) / chunks;
+    if (t1 == t0) continue;
+    e = run_scan(CrtProducer{res, L, size - 1}, size, out, size, sc, st, "crt_carry_scan", t0, t1);
+    if (e == cudaSuccess) e = done(t0 * kScanTile, std::min(size, t1 * kScanTile));
+  }
+  return e;
 }
 
 cudaError_t school_mul(const u64* a, u64 na, const u64* b, u64 nb, u64* out, Scan& sc, cudaStream_t st) {

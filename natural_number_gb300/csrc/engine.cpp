@@ -35,7 +35,7 @@ struct nn_context {
   // host-pointer calls: the second operand's copy runs on `copy` while the
   // first operand is transformed
   cudaStream_t copy = nullptr;
-  cudaEvent_t ev_first = nullptr, ev_second = nullptr;
+  cudaEvent_t ev_first = nullptr, ev_second = nullptr, ev_chunk = nullptr;
   u64 budget = 0;
   u64 held = 0;  // bytes of live allocations made through the context
   nn::Tables tables;
@@ -174,6 +174,25 @@ nn_status inverse_save(nn_context* c, nn_transform* t, u64* d_out, u64 size, u64
   return NN_OK;
 }
 
+// inverse_save(skip_last_pass) in normal mode, with the product's limbs
+// copied to h_out on the copy stream range by range as the carry scan
+// finishes them, so the copy-back overlaps the scan.
+constexpr int kCopyChunks = 8;
+nn_status inverse_save_to_host(nn_context* c, nn_transform* t, u64* d_out, u64 size, u64* h_out) {
+  const std::vector<nn::Pass> plan = c->passes(t->scale);
+  NN_CK(c, nn::ntt_inverse(t->res, t->scale, c->tables, c->stream, &plan, true), "inverse NTT");
+  const cudaError_t e =
+      nn::ntt_save_chunks(t->res, t->scale, d_out, size, c->scan, c->stream, kCopyChunks, [&](u64 lo, u64 hi) {
+        cudaError_t r = cudaEventRecord(c->ev_chunk, c->stream);
+        if (r == cudaSuccess) r = cudaStreamWaitEvent(c->copy, c->ev_chunk, 0);
+        if (r == cudaSuccess)
+          r = cudaMemcpyAsync(h_out + lo, d_out + lo, (hi - lo) * 8, cudaMemcpyDeviceToHost, c->copy);
+        return r;
+      });
+  NN_CK(c, e, "CRT/carry with copy-back");
+  return NN_OK;
+}
+
 nn_status pointwise(nn_context* c, nn_transform* dst, const nn_transform* a, const nn_transform* b) {
   if (a->scale != b->scale || a->scale < 2) {
     c->err = "pointwise: transforms differ in scale";
@@ -201,9 +220,11 @@ nn_status forward_fused(nn_context* c, nn_transform* t, const u64* d_limbs, u64 
 
 // Balanced NTT product at scale s into d_out (size limbs, or wrap).
 // b_ready (optional): an event b's contents wait for; the stream waits for it
-// only after a's forward transform.
+// only after a's forward transform.  h_out (optional): host memory the
+// product is also copied to, overlapping the carry scan; *h_done tells
+// whether that happened (fused pipelines only).
 nn_status ntt_product(nn_context* c, u64* d_out, const u64* a, u64 na, const u64* b, u64 nb, int s, u64 size,
-                      u64* written, cudaEvent_t b_ready = nullptr) {
+                      u64* written, cudaEvent_t b_ready = nullptr, u64* h_out = nullptr, bool* h_done = nullptr) {
   nn_transform xa, xb;
   nn_status st = forward(c, &xa, a, na, s);
   if (st == NN_OK && b_ready) {
@@ -212,7 +233,12 @@ nn_status ntt_product(nn_context* c, u64* d_out, const u64* a, u64 na, const u64
   }
   if (st == NN_OK && c->passes(s).size() >= 2) {
     st = forward_fused(c, &xb, b, nb, s, &xa);
-    if (st == NN_OK) st = inverse_save(c, &xb, d_out, size, written, true);
+    if (st == NN_OK && h_out && size - 1 <= (1ull << s)) {
+      st = inverse_save_to_host(c, &xb, d_out, size, h_out);
+      if (st == NN_OK && h_done) *h_done = true;
+    } else if (st == NN_OK) {
+      st = inverse_save(c, &xb, d_out, size, written, true);
+    }
   } else {
     if (st == NN_OK) st = forward(c, &xb, b, nb, s);
     if (st == NN_OK) st = pointwise(c, &xb, &xa, &xb);
@@ -226,7 +252,7 @@ nn_status ntt_product(nn_context* c, u64* d_out, const u64* a, u64 na, const u64
 // b_ready (optional): an event the contents of b wait for; the balanced NTT
 // product waits for it after a's forward transform, the other paths at once.
 nn_status mul_impl(nn_context* c, u64* d_out, const u64* a, u64 na, const u64* b, u64 nb,
-                   cudaEvent_t b_ready = nullptr) {
+                   cudaEvent_t b_ready = nullptr, u64* h_out = nullptr, bool* h_done = nullptr) {
   if (!d_out || !a || !b || na == 0 || nb == 0) {
     c->err = "mul: null pointer or empty operand";
     return NN_ERR_INVALID;
@@ -249,7 +275,7 @@ nn_status mul_impl(nn_context* c, u64* d_out, const u64* a, u64 na, const u64* b
   }
   // natural::_mul_NTT (natural.h:391-419)
   const int s = ntt_scale(na, nb), s_opt = ntt_scale(a0, nb);
-  if (s == s_opt) return ntt_product(c, d_out, a, na, b, nb, s, na + nb, nullptr, b_ready);
+  if (s == s_opt) return ntt_product(c, d_out, a, na, b, nb, s, na + nb, nullptr, b_ready, h_out, h_done);
   // Unbalanced: b's transform is made once at s_opt and reused for both
   // halves of a (mul_save_NTT_info / mul_load_NTT_info, natural.h:452-515).
   const u64 a1 = na - a0;
@@ -585,6 +611,7 @@ nn_status nn_context_create(int device, uint64_t budget, nn_context** out) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_first, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_second, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_chunk, cudaEventDisableTiming);
   if (e == cudaSuccess) e = nn::upload_primes();
   if (e == cudaSuccess) {
     cudaMemPool_t pool;
@@ -598,6 +625,7 @@ nn_status nn_context_create(int device, uint64_t budget, nn_context** out) {
   if (e != cudaSuccess) {
     nn_status st = e == cudaErrorNoDevice || e == cudaErrorNoKernelImageForDevice ? NN_ERR_NO_DEVICE : NN_ERR_CUDA;
     cudaGetLastError();
+    if (c->ev_chunk) cudaEventDestroy(c->ev_chunk);
     if (c->ev_second) cudaEventDestroy(c->ev_second);
     if (c->ev_first) cudaEventDestroy(c->ev_first);
     if (c->copy) cudaStreamDestroy(c->copy);
@@ -623,6 +651,7 @@ nn_status nn_context_destroy(nn_context* c) {
   nn::tables_free(c->tables);
   nn::scan_free(c->scan);
   cudaStreamSynchronize(c->copy);
+  cudaEventDestroy(c->ev_chunk);
   cudaEventDestroy(c->ev_second);
   cudaEventDestroy(c->ev_first);
   cudaStreamDestroy(c->copy);
@@ -757,13 +786,15 @@ nn_status nn_mul_host(nn_context* c, uint64_t* out, uint64_t* out_n, const uint6
   NN_CK(c, cudaStreamWaitEvent(c->copy, c->ev_first, 0), "copy stream wait");
   NN_CK(c, cudaMemcpyAsync(db, b, nb * 8, cudaMemcpyHostToDevice, c->copy), "H2D");
   NN_CK(c, cudaEventRecord(c->ev_second, c->copy), "event record");
-  st = mul_impl(c, dout, da, na, db, nb, c->ev_second);
+  bool copied = false;  // the balanced NTT path copies the product back while its carry scan runs
+  st = mul_impl(c, dout, da, na, db, nb, c->ev_second, out, &copied);
   if (st != NN_OK) {
     cudaStreamSynchronize(c->copy);
     return st;
   }
-  NN_CK(c, cudaMemcpyAsync(out, dout, (na + nb) * 8, cudaMemcpyDeviceToHost, c->stream), "D2H");
+  if (!copied) NN_CK(c, cudaMemcpyAsync(out, dout, (na + nb) * 8, cudaMemcpyDeviceToHost, c->stream), "D2H");
   st = nn_context_synchronize(c);
+  NN_CK(c, cudaStreamSynchronize(c->copy), "copy-back");
   if (st == NN_OK && out_n) *out_n = normalized(out, na + nb);
   return st;
 }

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -105,6 +106,11 @@ cudaError_t ntt_fused_last(u64* res, const u64* other, int s, const Tables& t, c
 // B^L - 1 in L limbs when size-1 > L (ntt_info.h:237-248).  Returns the
 // number of limbs written through *written (host value).
 cudaError_t ntt_save(const u64* res, int s, u64* out, u64 size, Scan& sc, u64* written, cudaStream_t st);
+// ntt_save in normal mode, run as `chunks` consecutive ranges of scan tiles;
+// after each range is launched, done(limb_begin, limb_end) is called with the
+// limbs that range writes (for instance to queue their copy to the host).
+cudaError_t ntt_save_chunks(const u64* res, int s, u64* out, u64 size, Scan& sc, cudaStream_t st, int chunks,
+                            const std::function<cudaError_t(u64, u64)>& done);
 // Schoolbook product by column sums + carry scan: out[0..na+nb).
 cudaError_t school_mul(const u64* a, u64 na, const u64* b, u64 nb, u64* out, Scan& sc, cudaStream_t st);
 // out[0..n) = x (nx limbs) + y (ny limbs) shifted up by `shift` limbs; the
