@@ -297,7 +297,7 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the uneven-size batch measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the served request stream")
-    ap.add_argument("--serve-jobs", type=int, default=300)
+    ap.add_argument("--serve-jobs", type=int, default=1000)
     ap.add_argument("--no-series", action="store_true", help="skip pi and e to 10^8 digits (a few seconds)")
     args = ap.parse_args()
     if args.impl == "reference":
