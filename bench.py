@@ -207,6 +207,37 @@ def measure_square(ctx, da, n: int, steps: int, warmup: int) -> dict:
             "frac": sqr_bytes / (ms / 1e3) / 1e9 / peak}
 
 
+def measure_division(ctx, reps: int = 3, cpu: bool = True) -> dict:
+    """A 2^22 / 2^21-limb division (natural::operator/ and %, the reference's
+    Newton division with every product on the GPU) through the host API,
+    checked by q*b + r == a on residues mod 2^64 -/+ 1; beside it the oracle
+    on one host core dividing 2^19 by 2^18 limbs (a bounded sample)."""
+    from natural_number_gb300.synth import limbs
+    from tests.gpu_util import mod_checks
+    n = 1 << 21
+    a, b = limbs(41, 2 * n), limbs(43, n)
+    q, r = ctx.div(a, b)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        q, r = ctx.div(a, b)
+    sec = (time.perf_counter() - t0) / reps
+    ma, mb, mq, mr = mod_checks(a), mod_checks(b), mod_checks(q), mod_checks(r)
+    exact = all((mq[i] * mb[i] + mr[i]) % m == ma[i] for i, m in enumerate((2**64 - 1, 2**64 + 1)))
+    out = {"workload": "%d-limb dividend by %d-limb divisor" % (2 * n, n), "seconds": sec,
+           "limbs_per_s": 3 * n / sec, "identity_check": bool(exact)}
+    if cpu:
+        from oracle import Oracle
+        o = Oracle("port")
+        m = 1 << 18
+        ca, cb = limbs(47, 2 * m), limbs(53, m)
+        t0 = time.perf_counter()
+        o.div(ca, cb)
+        cs = time.perf_counter() - t0
+        out["cpu_baseline"] = {"seconds": cs, "limbs_per_s": 3 * m / cs, "cores": 1, "kind": "port",
+                               "sample": "%d-limb dividend by %d-limb divisor" % (2 * m, m)}
+    return out
+
+
 def measure_series(ctx) -> dict:
     """pi and e to 10^8 digits (the reference's test.cpp recipes: pi with
     2^23 terms and a 6e6-limb square root, e with 2^24 terms), trees
@@ -299,6 +330,7 @@ def main() -> None:
     ap.add_argument("--no-serve", action="store_true", help="skip the served request stream")
     ap.add_argument("--serve-jobs", type=int, default=1000)
     ap.add_argument("--no-series", action="store_true", help="skip pi and e to 10^8 digits (a few seconds)")
+    ap.add_argument("--no-div", action="store_true", help="skip the 2^22 / 2^21-limb division")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -378,6 +410,7 @@ def main() -> None:
                "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 16 * n}
 
     square = measure_square(ctx, da, n, args.steps, args.warmup)
+    division = measure_division(ctx, cpu=not args.no_cpu) if rank == 0 and not args.no_div else None
 
     batched = None
     if not args.no_batch:
@@ -419,6 +452,8 @@ def main() -> None:
         "clocks": clk.summary(),
     }
     line["square"] = square
+    if division:
+        line["division"] = division
     if e2e:
         line["e2e"] = e2e
     if series:

@@ -81,7 +81,8 @@ def test_e_golden(ctx, golden, idx):
 
 def test_cpp_dropin_program(golden, tmp_path):
     """The C++ surface compiles unchanged-style user code and prints the
-    reference's 2^65536 (its demo program's output) and consistent q, r."""
+    reference's 2^65536 (its demo program's output), consistent q and r,
+    2000! and decimal / hex round trips."""
     import natural_number_gb300 as nn
     nn.lib()
     exe = tmp_path / "demo"
@@ -97,6 +98,7 @@ def test_cpp_dropin_program(golden, tmp_path):
     assert int(out[1], 16) == A // B and int(out[2]) == A % B
     import math
     assert int(out[4]) == math.factorial(2000)
+    assert out[5] == "dec ok" and out[6] == "hex ok"
 
 
 # Divisions on which the reference's own Newton division aborts
