@@ -208,23 +208,29 @@ def measure_square(ctx, da, n: int, steps: int, warmup: int) -> dict:
 
 
 def measure_division(ctx, reps: int = 3, cpu: bool = True) -> dict:
-    """A 2^22 / 2^21-limb division (natural::operator/ and %, the reference's
-    Newton division with every product on the GPU) through the host API,
-    checked by q*b + r == a on residues mod 2^64 -/+ 1; beside it the oracle
-    on one host core dividing 2^19 by 2^18 limbs (a bounded sample)."""
+    """A 2^22 / 2^21-limb division through the host API, twice: natural::_div
+    (the reference's Newton steps, every product on the GPU) and the division
+    with every step on the GPU (nn_divmod_host); both checked by q*b + r == a
+    on residues mod 2^64 -/+ 1.  Beside them the oracle on one host core
+    dividing 2^19 by 2^18 limbs (a bounded sample)."""
     from natural_number_gb300.synth import limbs
     from tests.gpu_util import mod_checks
     n = 1 << 21
     a, b = limbs(41, 2 * n), limbs(43, n)
-    q, r = ctx.div(a, b)
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        q, r = ctx.div(a, b)
-    sec = (time.perf_counter() - t0) / reps
-    ma, mb, mq, mr = mod_checks(a), mod_checks(b), mod_checks(q), mod_checks(r)
-    exact = all((mq[i] * mb[i] + mr[i]) % m == ma[i] for i, m in enumerate((2**64 - 1, 2**64 + 1)))
-    out = {"workload": "%d-limb dividend by %d-limb divisor" % (2 * n, n), "seconds": sec,
-           "limbs_per_s": 3 * n / sec, "identity_check": bool(exact)}
+    ma, mb = mod_checks(a), mod_checks(b)
+
+    def run(fn):
+        q, r = fn(a, b)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            q, r = fn(a, b)
+        sec = (time.perf_counter() - t0) / reps
+        mq, mr = mod_checks(q), mod_checks(r)
+        ok = all((mq[i] * mb[i] + mr[i]) % m == ma[i] for i, m in enumerate((2**64 - 1, 2**64 + 1)))
+        return {"seconds": sec, "limbs_per_s": 3 * n / sec, "identity_check": bool(ok)}
+
+    out = {"workload": "%d-limb dividend by %d-limb divisor" % (2 * n, n),
+           "natural_div": run(ctx.div), "device": run(ctx.divmod)}
     if cpu:
         from oracle import Oracle
         o = Oracle("port")

@@ -94,6 +94,17 @@ nn_status nn_sqr(nn_context* ctx, uint64_t* d_out, const uint64_t* d_a, uint64_t
  * n_a, n_b <= 2^scale.  d_out: max(size, 2^scale) limbs; *written as above. */
 nn_status nn_ntt_mul(nn_context* ctx, uint64_t* d_out, const uint64_t* d_a, uint64_t n_a, const uint64_t* d_b,
                      uint64_t n_b, int scale, uint64_t size, uint64_t* written);
+/* Quotient and remainder with every step on the GPU: an exact Newton division
+ * of this build's own (normalisation, a Newton reciprocal with precision
+ * doubling, one quotient estimate and at most a few corrections).  Quotient
+ * and remainder are unique, so they equal natural::_div's (natural.h:749-769).
+ * q gets n_a - n_b + 1 limbs and r n_b limbs, not normalised; n_a >= n_b >= 1
+ * and the divisor's top limb is nonzero.  nn_div takes device pointers and
+ * returns when done; nn_divmod_host takes host pointers. */
+nn_status nn_div(nn_context* ctx, uint64_t* d_q, uint64_t* d_r, const uint64_t* d_a, uint64_t n_a,
+                 const uint64_t* d_b, uint64_t n_b);
+nn_status nn_divmod_host(nn_context* ctx, uint64_t* q, uint64_t* r, const uint64_t* a, uint64_t n_a,
+                         const uint64_t* b, uint64_t n_b);
 /* Schoolbook product (asmMul1 / mul_base, base.h:56-81) on the GPU: n_a+n_b limbs. */
 nn_status nn_mul_base(nn_context* ctx, uint64_t* d_out, const uint64_t* d_a, uint64_t n_a, const uint64_t* d_b,
                       uint64_t n_b);

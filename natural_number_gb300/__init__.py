@@ -46,6 +46,12 @@ class MulJob(C.Structure):
                 ("d_out", C.c_void_p)]
 
 
+def _trim(x: np.ndarray) -> np.ndarray:
+    """Drops leading zero limbs, keeping at least one (natural::std)."""
+    nz = np.flatnonzero(x)
+    return x[: (int(nz[-1]) + 1) if nz.size else 1]
+
+
 class NNError(RuntimeError):
     def __init__(self, status: int, msg: str):
         super().__init__(f"{msg} (status {status})")
@@ -119,6 +125,8 @@ def lib() -> C.CDLL:
         "nn_div_host": (C.c_int, [_vp, _u64p, C.c_uint64, _u64p, C.c_uint64, C.POINTER(_u64p), _u64p,
                                   C.POINTER(_u64p), _u64p]),
         "nn_pow_host": (C.c_int, [_vp, _u64p, C.c_uint64, C.c_uint64, C.POINTER(_u64p), _u64p]),
+        "nn_div": (C.c_int, [_vp, _vp, _vp, _vp, C.c_uint64, _vp, C.c_uint64]),
+        "nn_divmod_host": (C.c_int, [_vp, _u64p, _u64p, _u64p, C.c_uint64, _u64p, C.c_uint64]),
         "nn_reciprocal_host": (C.c_int, [_vp, _u64p, C.c_uint64, C.c_uint64, C.c_int, C.POINTER(_u64p), _u64p]),
         "nn_to_dec_host": (C.c_int, [_vp, _u64p, C.c_uint64, C.POINTER(_vp), _u64p]),
         "nn_pi_dec_host": (C.c_int, [_vp, C.c_uint64, C.c_uint64, C.c_uint64, C.POINTER(_vp), _u64p]),
@@ -257,6 +265,15 @@ class Context:
                                       C.byref(r), C.byref(rn)), "div")
         return self._take(q, qn.value), self._take(r, rn.value)
 
+    def divmod(self, a, b) -> tuple[np.ndarray, np.ndarray]:
+        """Quotient and remainder by the division with every step on the GPU
+        (nn_divmod_host), normalised; the divisor's top limb must be nonzero."""
+        a, b = _np(a), _np(b)
+        q = np.zeros(a.size - b.size + 1, dtype=np.uint64)
+        r = np.zeros(b.size, dtype=np.uint64)
+        self._check(lib().nn_divmod_host(self.h, _ptr(q), _ptr(r), _ptr(a), a.size, _ptr(b), b.size), "divmod")
+        return _trim(q), _trim(r)
+
     def pow(self, b, e: int) -> np.ndarray:
         b = _np(b)
         p, n = _u64p(), C.c_uint64()
@@ -318,6 +335,11 @@ class Context:
     def sqr_device(self, out, a, n: int | None = None) -> None:
         n = a.numel() if n is None else n
         self._check(lib().nn_sqr(self.h, _vp(_dptr(out)), _vp(_dptr(a)), n), "nn_sqr")
+
+    def div_device(self, q, r, a, b) -> None:
+        """nn_div on device tensors: q (n_a - n_b + 1 limbs) and r (n_b limbs)."""
+        self._check(lib().nn_div(self.h, _vp(_dptr(q)), _vp(_dptr(r)), _vp(_dptr(a)), a.numel(), _vp(_dptr(b)),
+                                 b.numel()), "nn_div")
 
     def mul_base_device(self, out, a, b) -> None:
         self._check(lib().nn_mul_base(self.h, _vp(_dptr(out)), _vp(_dptr(a)), a.numel(), _vp(_dptr(b)), b.numel()),

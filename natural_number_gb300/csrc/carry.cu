@@ -83,6 +83,17 @@ __global__ void __launch_bounds__(1024) wrap_fix_kernel(u64* out, u64 L, const u
   }
 }
 
+// out[0..n] = in[0..n) << cl and out[0..n) = in[0..n) >> cl, 1 <= cl <= 63
+// (asmShl / asmShr, asm.h:31-33); out does not overlap in.
+__global__ void shl_bits_kernel(u64* out, const u64* in, u64 n, unsigned cl) {
+  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += (u64)gridDim.x * blockDim.x)
+    out[i] = (i < n ? in[i] << cl : 0) | (i > 0 ? in[i - 1] >> (64 - cl) : 0);
+}
+__global__ void shr_bits_kernel(u64* out, const u64* in, u64 n, unsigned cl) {
+  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x)
+    out[i] = (in[i] >> cl) | (i + 1 < n ? in[i + 1] << (64 - cl) : 0);
+}
+
 // The lookback's bounded wait on a status word that nothing sets: after
 // `limit` polls it gives up and records the error, as a scan tile does.
 __global__ void wait_probe_kernel(const u32* flag, u32* err, int limit) {
@@ -187,6 +198,35 @@ cudaError_t add_shifted(const u64* x, u64 nx, const u64* y, u64 ny, u64 shift, u
   cudaError_t e = scan_reserve(sc, 1);
   if (e != cudaSuccess) return e;
   return run_scan(AddProducer{x, nx, y, ny, shift}, n, out, n, sc, st, "add_scan");
+}
+
+cudaError_t lin_combine(u64* out, u64 n_out, const u64* x, u64 nx, u64 xs, const u64* y, u64 ny, u64 ys, bool sub,
+                        int cin, Scan& sc, cudaStream_t st, const u64* flip) {
+  cudaError_t e = scan_reserve(sc, 1);
+  if (e != cudaSuccess) return e;
+  return run_scan(LinProducer{x, nx, xs, y, ny, ys, n_out, sub ? 1 : 0, cin, flip}, n_out + 1, out, n_out + 1, sc,
+                  st, sub ? "sub_scan" : "add_scan");
+}
+
+cudaError_t shl_bits(u64* out, const u64* in, u64 n, unsigned cl, cudaStream_t st) {
+  if (cl == 0) {
+    cudaError_t e = cudaMemcpyAsync(out, in, n * 8, cudaMemcpyDeviceToDevice, st);
+    return e == cudaSuccess ? cudaMemsetAsync(out + n, 0, 8, st) : e;
+  }
+  const unsigned blocks = (unsigned)std::min<u64>((n + 1 + 255) / 256, 152 * 16);
+  launch_begin("shift_bits", st);
+  shl_bits_kernel<<<blocks, 256, 0, st>>>(out, in, n, cl);
+  launch_end(st);
+  return cudaGetLastError();
+}
+
+cudaError_t shr_bits(u64* out, const u64* in, u64 n, unsigned cl, cudaStream_t st) {
+  if (cl == 0) return cudaMemcpyAsync(out, in, n * 8, cudaMemcpyDeviceToDevice, st);
+  const unsigned blocks = (unsigned)std::min<u64>((n + 255) / 256, 152 * 16);
+  launch_begin("shift_bits", st);
+  shr_bits_kernel<<<blocks, 256, 0, st>>>(out, in, n, cl);
+  launch_end(st);
+  return cudaGetLastError();
 }
 
 cudaError_t wait_probe(Scan& sc, int limit, cudaStream_t st) {

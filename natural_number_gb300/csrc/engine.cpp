@@ -517,6 +517,20 @@ u64 normalized(const u64* x, u64 n) {  // natural::std (natural.h:82-93)
 
 }  // namespace
 
+// Context access for the other host translation units (context_access.h).
+namespace nn {
+cudaStream_t ctx_stream(nn_context* c) { return c->stream; }
+Scan& ctx_scan(nn_context* c) { return c->scan; }
+nn_status ctx_alloc(nn_context* c, u64** p, u64 words) { return dev_alloc(c, p, words); }
+void ctx_free(nn_context* c, u64* p, u64 words) { dev_free(c, p, words); }
+nn_status ctx_mul(nn_context* c, u64* out, const u64* a, u64 na, const u64* b, u64 nb) {
+  return mul_impl(c, out, a, na, b, nb);
+}
+nn_status ctx_fail(nn_context* c, cudaError_t e, const char* what) { return fail(c, e, what); }
+void ctx_error(nn_context* c, const char* msg) { c->err = msg; }
+nn_status ctx_scratch(nn_context* c, int slot, u64 words, u64** p) { return scratch(c, slot, words, p); }
+}  // namespace nn
+
 // Page-locked host blocks for limb buffers, recycled by size (cudaMallocHost
 // pins pages and is far too slow to call per buffer).  Intentionally never
 // destroyed: blocks may be freed during static destruction.

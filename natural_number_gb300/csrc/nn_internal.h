@@ -119,6 +119,18 @@ cudaError_t school_mul(const u64* a, u64 na, const u64* b, u64 nb, u64* out, Sca
 cudaError_t add_shifted(const u64* x, u64 nx, const u64* y, u64 ny, u64 shift, u64* out, u64 n, Scan& sc,
                         cudaStream_t st);
 
+// out[0..n_out) = x*B^xs + y*B^ys (sub = false) or x*B^xs - y*B^ys - (1 - cin)
+// modulo B^n_out (sub = true), and out[n_out] = the carry out of the top limb
+// (for a subtraction with cin = 1: 1 exactly when x*B^xs >= y*B^ys).  out
+// holds n_out + 1 limbs and does not alias x or y.  A nonzero *flip (device
+// memory, when flip is given) swaps add and subtract.
+cudaError_t lin_combine(u64* out, u64 n_out, const u64* x, u64 nx, u64 xs, const u64* y, u64 ny, u64 ys, bool sub,
+                        int cin, Scan& sc, cudaStream_t st, const u64* flip = nullptr);
+// out[0..n] = in << cl (n + 1 limbs) and out[0..n) = in >> cl, 0 <= cl <= 63;
+// out does not overlap in.
+cudaError_t shl_bits(u64* out, const u64* in, u64 n, unsigned cl, cudaStream_t st);
+cudaError_t shr_bits(u64* out, const u64* in, u64 n, unsigned cl, cudaStream_t st);
+
 // Runs the carry lookback's bounded wait on a status word nothing sets (at
 // most `limit` polls); it gives up and sets sc.err, which the host reads.
 cudaError_t wait_probe(Scan& sc, int limit, cudaStream_t st);

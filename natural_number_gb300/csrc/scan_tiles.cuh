@@ -135,6 +135,40 @@ struct AddProducer {
   }
 };
 
+// x*B^xs + y*B^ys (add) or, as x*B^xs + ~(y*B^ys) + cin over `count`
+// positions (sub), x*B^xs - y*B^ys - (1 - cin): with the scan run over
+// count + 1 positions, the extra limb receives the carry out, which for a
+// subtraction is 1 exactly when no borrow occurred.  Zero beyond count.
+// With `flip` set, a nonzero *flip (a limb in device memory, read by every
+// thread) swaps add and subtract, so a sign known only on the device picks
+// the operation without a round trip to the host.
+struct LinProducer {
+  static constexpr bool kBulk = false;
+  __device__ __forceinline__ void bulk(u64, W3 (&)[kScanE]) const {}
+  const u64* x;
+  u64 nx, xs;
+  const u64* y;
+  u64 ny, ys;
+  u64 count;
+  int sub, cin;
+  const u64* flip;
+  __device__ __forceinline__ W3 operator()(u64 k) const {
+    if (k >= count) return W3{0, 0, 0};
+    const u64 a = (k >= xs && k - xs < nx) ? x[k - xs] : 0;
+    u64 b = (k >= ys && k - ys < ny) ? y[k - ys] : 0;
+    u64 c = 0;
+    if (sub ^ (flip != nullptr && __ldcg(flip) != 0)) {
+      b = ~b;
+      c = k == 0 ? (u64)cin : 0;
+    }
+    const u64 s = a + b;
+    const u64 c1 = s < a;
+    const u64 s2 = s + c;
+    const u64 c2 = s2 < s;
+    return W3{s2, c1 + c2, 0};
+  }
+};
+
 __device__ __forceinline__ u32 flag_load(const u32* f) {
   u32 v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(f) : "memory");

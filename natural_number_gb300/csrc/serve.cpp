@@ -219,6 +219,15 @@ void scheduler(nn_server* S) {
   }
 }
 
+// Divisions whose divisor has at least this many limbs run with every step on
+// the GPU (nn_divmod_host); shorter ones take natural::_div on the host.
+constexpr uint64_t kDeviceDivLimbs = 1024;
+
+uint64_t trimmed(const uint64_t* x, uint64_t n) {
+  while (n > 1 && x[n - 1] == 0) --n;
+  return n;
+}
+
 void div_worker(nn_server* S, int w) {
   cudaSetDevice(S->device);
   nn_context* c = S->div_ctx[w];
@@ -236,16 +245,28 @@ void div_worker(nn_server* S, int w) {
       S->div_running += 1;
     }
     nn_status st = NN_OK;
-    uint64_t *q = nullptr, *r = nullptr, qn = 0, rn = 0;
-    st = nn_div_host(c, R->a, R->na, R->b, R->nb, &q, &qn, &r, &rn);
-    if (st == NN_OK) {
-      std::memcpy(R->q, q, 8 * qn);
-      std::memcpy(R->r, r, 8 * rn);
-      R->q_n = qn;
-      R->r_n = rn;
+    uint64_t na = R->na, nb = R->nb;
+    while (na > 1 && R->a[na - 1] == 0) --na;
+    while (nb > 1 && R->b[nb - 1] == 0) --nb;
+    if (nb >= kDeviceDivLimbs && na >= nb) {
+      // long divisors: every step on the GPU (nn_divmod_host); normalised results
+      st = nn_divmod_host(c, R->q, R->r, R->a, na, R->b, nb);
+      if (st == NN_OK) {
+        R->q_n = trimmed(R->q, na - nb + 1);
+        R->r_n = trimmed(R->r, nb);
+      }
+    } else {
+      uint64_t *q = nullptr, *r = nullptr, qn = 0, rn = 0;
+      st = nn_div_host(c, R->a, R->na, R->b, R->nb, &q, &qn, &r, &rn);
+      if (st == NN_OK) {
+        std::memcpy(R->q, q, 8 * qn);
+        std::memcpy(R->r, r, 8 * rn);
+        R->q_n = qn;
+        R->r_n = rn;
+      }
+      nn_free(q);
+      nn_free(r);
     }
-    nn_free(q);
-    nn_free(r);
     {
       std::lock_guard<std::mutex> lk(S->mu);
       finish(S, R, st);

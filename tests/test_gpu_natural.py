@@ -167,3 +167,64 @@ def test_levels_1e7_and_1e8_digits(ctx, golden, kind):
         assert len(s) == c["out"]["len"]
         assert hashlib.sha256(s.encode()).hexdigest() == c["out"]["sha256"]
         del s
+
+
+def _int(x):
+    return int.from_bytes(np.ascontiguousarray(x, dtype="<u8").tobytes(), "little")
+
+
+def _limbs_of(v, n=None):
+    n = n or max(1, (v.bit_length() + 63) // 64)
+    return np.frombuffer(v.to_bytes(8 * n, "little"), dtype="<u8").astype(np.uint64)
+
+
+def _check_divmod(ctx, x, y, q, r):
+    """q, r = divmod(x, y): exactly by Python for small operands, else by
+    q*y + r == x with the GPU product (tested on its own) and r < y."""
+    Q, R = _int(q), _int(r)
+    if x.bit_length() <= 64 * 20000:
+        assert Q == x // y and R == x % y
+    else:
+        assert R < y
+        assert _int(ctx.mul(q, _limbs_of(y))) + R == x
+
+
+@pytest.mark.parametrize("na,nb", [(2048, 1024), (5000, 1024), (100000, 3000), (1 << 18, 1 << 17), (3000, 2999),
+                                   ((1 << 16) + 5, 1030), (1024, 1024), (4000, 33), (70, 5)])
+def test_device_division_vs_python(ctx, na, nb):
+    """The division with every step on the GPU (nn_divmod_host, nn_div):
+    quotient and remainder as Python's for short and long quotients,
+    power-of-two, all-ones and near-multiple divisors."""
+    import torch
+    a, b = limbs(na * 7 + 1, na), limbs(nb * 11 + 3, nb)
+    A, Bv = _int(a), _int(b)
+    cases = [(A, Bv), (A, 1 << (64 * nb - 1)), (A, (1 << (64 * nb)) - 1), (A, Bv | 1)]
+    if na <= 20000:  # exact multiples and one below need Python products of the full size
+        cases += [(Bv * (A >> (64 * nb)), Bv), (Bv * (A >> (64 * nb)) - 1, Bv)]
+    for x, y in cases:
+        if x < 0:
+            continue
+        xa, ya = _limbs_of(x), _limbs_of(y)
+        if xa.size < ya.size:
+            continue
+        q, r = ctx.divmod(xa, ya)
+        _check_divmod(ctx, x, y, q, r)
+    # device pointers
+    dq = torch.zeros(na - nb + 1, dtype=torch.uint64, device="cuda")
+    dr = torch.zeros(nb, dtype=torch.uint64, device="cuda")
+    ctx.div_device(dq, dr, to_dev_np(a), to_dev_np(b))
+    _check_divmod(ctx, A, Bv, dq.cpu().numpy(), dr.cpu().numpy())
+
+
+def to_dev_np(x):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(x)).to("cuda")
+
+
+def test_device_division_on_reference_abort_inputs(ctx):
+    """The GPU division also handles the inputs on which the reference's own
+    division aborts, and large 2n-by-n cases."""
+    for sa, na, sb, nb in REFERENCE_ABORTS + [(7, 9000, 8, 4500), (9, 300000, 10, 150000)]:
+        a, b = limbs(sa, na), limbs(sb, nb)
+        q, r = ctx.divmod(a, b)
+        _check_divmod(ctx, _int(a), _int(b), q, r)

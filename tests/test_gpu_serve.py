@@ -10,6 +10,11 @@ from natural_number_gb300.synth import limbs, log_uniform_sizes
 pytestmark = pytest.mark.gpu
 
 
+def _norm(x):
+    nz = np.flatnonzero(x)
+    return x[: (int(nz[-1]) + 1) if nz.size else 1]
+
+
 def _mix(n, seed, lo=3, hi=15):
     rng = np.random.default_rng(seed)
     sizes = log_uniform_sizes(seed, 2 * n, lo, hi)
@@ -41,7 +46,7 @@ def test_served_results_equal_alone_results(oracle):
             assert np.array_equal(res, oracle.mul(a, b))
         else:
             q, r = oracle.div(a, b)
-            assert np.array_equal(res[0], q) and np.array_equal(res[1], r)
+            assert np.array_equal(_norm(res[0]), _norm(q)) and np.array_equal(_norm(res[1]), _norm(r))
         assert meta["submit"] <= meta["admit"] <= meta["done"]
     assert stats["batches"] >= 1
 
