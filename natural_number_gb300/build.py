@@ -24,7 +24,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["ntt.cu", "carry.cu", "batch.cu", "noalloc.cu"]
 CPP_SOURCES = ["engine.cpp", "profile.cpp", "natural_ops.cpp", "serve.cpp", "series.cpp", "host_glue.cpp", "divide.cpp"]
-HEADERS = ["nn_device.cuh", "nn_internal.h", "ntt_tiles.cuh", "scan_tiles.cuh", "../../include/natural_gb300.hpp"]
+HEADERS = ["nn_device.cuh", "nn_internal.h", "ntt_tiles.cuh", "scan_tiles.cuh", "context_access.h",
+           "../../include/natural_gb300.hpp"]
 
 
 def _newer(target: str, deps: list[str]) -> bool:

@@ -22,6 +22,7 @@
 // limb read back.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <bit>
 #include <cstring>
 #include <vector>
@@ -64,10 +65,70 @@ struct Buf {
     if (_s != NN_OK) return _s;      \
   } while (0)
 
+// Page-locked staging for the division's small host<->device transfers (limbs
+// read back for comparisons, constants, the base-case reciprocal): per host
+// thread, grown on demand, never released.
+u64* staging(u64 words) {
+  static thread_local u64* buf = nullptr;
+  static thread_local u64 cap = 0;
+  if (cap < words) {
+    if (buf) nn_host_free(buf, cap * 8);
+    cap = std::max<u64>(words, 256);
+    buf = static_cast<u64*>(nn_host_alloc(cap * 8));
+    if (!buf) cap = 0;
+  }
+  return buf;
+}
+
+// A host buffer as the GPU copies see it: the buffer itself when it is
+// page-locked, else a page-locked block from the library's pool, filled from
+// (load) or emptied into (store) the caller's buffer on all host cores.
+struct HostStage {
+  u64* user;
+  u64 n;
+  u64* p;
+  bool own = false;
+  HostStage(const u64* buf, u64 words) : user(const_cast<u64*>(buf)), n(words), p(const_cast<u64*>(buf)) {
+    cudaPointerAttributes at{};
+    const bool locked = cudaPointerGetAttributes(&at, buf) == cudaSuccess && at.type == cudaMemoryTypeHost;
+    cudaGetLastError();
+    if (!locked) {
+      p = static_cast<u64*>(nn_host_alloc(words * 8));
+      own = true;
+    }
+  }
+  HostStage(const HostStage&) = delete;
+  HostStage& operator=(const HostStage&) = delete;
+  bool ok() const { return p != nullptr; }
+  void load() {
+    if (own) nn_host_copy(p, user, n);
+  }
+  void store() {
+    if (own) nn_host_copy(user, p, n);
+  }
+  ~HostStage() {
+    if (own && p) nn_host_free(p, n * 8);
+  }
+};
+
 nn_status read_limb(nn_context* c, const u64* p, u64* v) {
   cudaStream_t st = nn::ctx_stream(c);
-  DV_CK(c, cudaMemcpyAsync(v, p, 8, cudaMemcpyDeviceToHost, st), "read limb");
+  u64* h = staging(1);
+  if (!h) return NN_ERR_OOM;
+  DV_CK(c, cudaMemcpyAsync(h, p, 8, cudaMemcpyDeviceToHost, st), "read limb");
   DV_CK(c, cudaStreamSynchronize(st), "read limb");
+  *v = h[0];
+  return NN_OK;
+}
+
+// Copies n host limbs to the device through the staging buffer and waits.
+nn_status put_limbs(nn_context* c, u64* d, const u64* h, u64 n) {
+  cudaStream_t st = nn::ctx_stream(c);
+  u64* s = staging(n);
+  if (!s) return NN_ERR_OOM;
+  std::memcpy(s, h, n * 8);
+  DV_CK(c, cudaMemcpyAsync(d, s, n * 8, cudaMemcpyHostToDevice, st), "constants");
+  DV_CK(c, cudaStreamSynchronize(st), "constants");
   return NN_OK;
 }
 
@@ -121,12 +182,13 @@ nn_status recip(nn_context* c, const u64* d, u64 t, u64* x) {
   nn::Scan& sc = nn::ctx_scan(c);
   if (t <= kRecipBase) {
     std::vector<u64> hd(t), hx(t + 2, 0);
-    DV_CK(c, cudaMemcpyAsync(hd.data(), d, t * 8, cudaMemcpyDeviceToHost, st), "reciprocal base");
+    u64* s = staging(t);
+    if (!s) return NN_ERR_OOM;
+    DV_CK(c, cudaMemcpyAsync(s, d, t * 8, cudaMemcpyDeviceToHost, st), "reciprocal base");
     DV_CK(c, cudaStreamSynchronize(st), "reciprocal base");
+    std::memcpy(hd.data(), s, t * 8);
     recip_base(hd.data(), t, hx.data());
-    DV_CK(c, cudaMemcpyAsync(x, hx.data(), (t + 2) * 8, cudaMemcpyHostToDevice, st), "reciprocal base");
-    DV_CK(c, cudaStreamSynchronize(st), "reciprocal base");
-    return NN_OK;
+    return put_limbs(c, x, hx.data(), t + 2);
   }
   const u64 h = (t + 1) / 2 + 1;
   Buf xh(c), p(c), e(c), y(c);
@@ -193,7 +255,7 @@ nn_status div_impl(nn_context* c, u64* q, u64* r, const u64* a, u64 na, const u6
   // q1 = q' - 2 (0 when q' < 2): never above q
   DV_ST(small.alloc(2));
   const u64 consts[2] = {2, 0};
-  DV_CK(c, cudaMemcpyAsync(small.p, consts, 16, cudaMemcpyHostToDevice, st), "constant");
+  DV_ST(put_limbs(c, small.p, consts, 2));
   DV_ST(q1.alloc(k + 1));
   DV_CK(c, nn::lin_combine(q1.p, k, qe, k, 0, small.p, 1, 0, true, 1, sc, st), "quotient estimate");
   u64 ge2 = 0;
@@ -228,13 +290,12 @@ nn_status div_impl(nn_context* c, u64* q, u64* r, const u64* a, u64 na, const u6
   }
   // q = q1 + count: the quotient fits na - nb + 1 limbs
   const u64 cnt[2] = {count, 0};
-  DV_CK(c, cudaMemcpyAsync(small.p, cnt, 16, cudaMemcpyHostToDevice, st), "constant");
+  DV_ST(put_limbs(c, small.p, cnt, 2));
   DV_ST(qs.alloc(k + 1));
   DV_CK(c, nn::lin_combine(qs.p, k, q1.p, k, 0, small.p, 1, 0, false, 0, sc, st), "quotient");
   DV_CK(c, cudaMemcpyAsync(q, qs.p, (na - nb + 1) * 8, cudaMemcpyDeviceToDevice, st), "quotient");
   // r = (A - q D) >> cl  (below D: nb limbs)
   DV_CK(c, nn::shr_bits(r, cur, nb, cl, st), "remainder");
-  DV_CK(c, cudaStreamSynchronize(st), "division");  // the small host constants must outlive their copies
   return NN_OK;
 }
 
@@ -258,12 +319,24 @@ nn_status nn_divmod_host(nn_context* c, uint64_t* q, uint64_t* r, const uint64_t
   Buf dq(c), dr(c);
   DV_ST(dq.alloc(n_a - n_b + 1));
   DV_ST(dr.alloc(n_b));
-  DV_CK(c, cudaMemcpyAsync(da, a, n_a * 8, cudaMemcpyHostToDevice, st), "H2D");
-  DV_CK(c, cudaMemcpyAsync(db, b, n_b * 8, cudaMemcpyHostToDevice, st), "H2D");
+  // Pageable host buffers move through page-locked staging blocks, page-locked
+  // ones directly: after large pageable transfers elsewhere in the process the
+  // driver's own staging of pageable copies was measured several times slower.
+  HostStage sa(a, n_a), sb(b, n_b), sq(q, n_a - n_b + 1), sr(r, n_b);
+  if (!sa.ok() || !sb.ok() || !sq.ok() || !sr.ok()) return NN_ERR_OOM;
+  sa.load();
+  sb.load();
+  DV_CK(c, cudaMemcpyAsync(da, sa.p, n_a * 8, cudaMemcpyHostToDevice, st), "H2D");
+  DV_CK(c, cudaMemcpyAsync(db, sb.p, n_b * 8, cudaMemcpyHostToDevice, st), "H2D");
   DV_ST(div_impl(c, dq.p, dr.p, da, n_a, db, n_b));
-  DV_CK(c, cudaMemcpyAsync(q, dq.p, (n_a - n_b + 1) * 8, cudaMemcpyDeviceToHost, st), "D2H");
-  DV_CK(c, cudaMemcpyAsync(r, dr.p, n_b * 8, cudaMemcpyDeviceToHost, st), "D2H");
-  return nn_context_synchronize(c);
+  DV_CK(c, cudaMemcpyAsync(sq.p, dq.p, (n_a - n_b + 1) * 8, cudaMemcpyDeviceToHost, st), "D2H");
+  DV_CK(c, cudaMemcpyAsync(sr.p, dr.p, n_b * 8, cudaMemcpyDeviceToHost, st), "D2H");
+  const nn_status status = nn_context_synchronize(c);
+  if (status == NN_OK) {
+    sq.store();
+    sr.store();
+  }
+  return status;
 }
 
 nn_status nn_div(nn_context* c, uint64_t* d_q, uint64_t* d_r, const uint64_t* d_a, uint64_t n_a,
