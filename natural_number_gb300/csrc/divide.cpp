@@ -14,7 +14,8 @@
 //      (one guard limb, so the Newton error squared is divided by B and V is
 //      within one unit of the floor, never above it); t <= 32 is Knuth's
 //      algorithm D on the host;
-//   3. q' = floor(A_top V / B^(2t)) - 2 is at most q and at least q - 3;
+//   3. floor(A_top V / B^(2t)) is within one of q, so q' = that - 2 lies in
+//      [q - 3, q - 1];
 //   4. r = A - q' D, then at most a few steps r -= D, q' += 1 while r >= D;
 //   5. r >>= cl.
 // Every product is the engine's (natural::_mul dispatch); sums, differences
