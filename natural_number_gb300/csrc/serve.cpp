@@ -74,6 +74,7 @@ struct nn_server {
   std::vector<cudaStream_t> streams;
   int next_stream = 0;
   std::vector<nn_context*> div_ctx;
+  std::vector<cudaStream_t> div_streams;  // the division contexts' low-priority streams
   std::mutex mu;
   std::condition_variable cv, done_cv, div_cv;
   std::deque<Request*> waiting;
@@ -314,10 +315,15 @@ nn_status nn_server_create(int device, uint64_t hbm_budget, int streams, int div
     delete S;
     return st;
   }
+  // Product batches run on high-priority streams and divisions (long chains
+  // of dependent kernels on the worker contexts) on low-priority ones, so a
+  // batch that arrives while a division runs gets the SMs as they free up.
+  int least = 0, greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&least, &greatest);
   streams = std::max(1, std::min(streams, 16));
   for (int i = 0; i < streams; ++i) {
     cudaStream_t s;
-    cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, greatest);
     S->streams.push_back(s);
   }
   div_workers = std::max(1, std::min(div_workers, 8));
@@ -325,10 +331,16 @@ nn_status nn_server_create(int device, uint64_t hbm_budget, int streams, int div
     nn_context* c = nullptr;
     st = nn_context_create(device, 0, &c);
     if (st != NN_OK) break;
+    cudaStream_t low = nullptr;
+    cudaStreamCreateWithPriority(&low, cudaStreamNonBlocking, least);
+    nn_context_set_stream(c, low);
+    S->div_streams.push_back(low);
     S->div_ctx.push_back(c);
   }
   if (st != NN_OK) {
     for (nn_context* c : S->div_ctx) nn_context_destroy(c);
+    for (cudaStream_t s : S->div_streams) cudaStreamDestroy(s);
+    for (cudaStream_t s : S->streams) cudaStreamDestroy(s);
     nn_context_destroy(S->ctx);
     delete S;
     return st;
@@ -420,7 +432,8 @@ nn_status nn_server_destroy(nn_server* S) {
   for (cudaStream_t s : S->streams) cudaStreamSynchronize(s);
   nn_context_use_own_stream(S->ctx);  // the context must not keep a handle to a stream destroyed below
   for (cudaStream_t s : S->streams) cudaStreamDestroy(s);
-  for (nn_context* c : S->div_ctx) nn_context_destroy(c);
+  for (nn_context* c : S->div_ctx) nn_context_destroy(c);  // waits on its stream, then drops it
+  for (cudaStream_t s : S->div_streams) cudaStreamDestroy(s);
   nn_context_destroy(S->ctx);
   delete S;
   return NN_OK;
