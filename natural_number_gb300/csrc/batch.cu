@@ -25,7 +25,6 @@ NN_DEFINE_PRIME_UPLOADER(upload_primes_batch)
 namespace {
 
 constexpr int kWaitLimit = 1 << 24;
-constexpr u64 kPointwiseChunk = 1024;  // groups of 4 residues per pointwise item
 
 __device__ __forceinline__ u32 ld_acquire(const u32* p) {
   u32 v;
@@ -39,16 +38,20 @@ __device__ __forceinline__ void run_pass(u64* sm, const BatchJob& J, const Batch
   const int pk = it.pass;
   const int s = J.s, l0 = J.lambda0[pk], R = J.R[pk];
   const u64* tab = INV ? t.iroot : t.root;
-  if (J.C[pk] == 16) {
-    if (first)
-      pass_tile<16, true, INV, SCALE, true>(sm, in, out, n_in, s, l0, R, tab, t.cap, it.prime, it.tile);
-    else
-      pass_tile<16, false, INV, SCALE, true>(sm, in, out, n_in, s, l0, R, tab, t.cap, it.prime, it.tile);
-  } else {
-    if (first)
-      pass_tile<2, true, INV, SCALE, true>(sm, in, out, n_in, s, l0, R, tab, t.cap, it.prime, it.tile);
-    else
-      pass_tile<2, false, INV, SCALE, true>(sm, in, out, n_in, s, l0, R, tab, t.cap, it.prime, it.tile);
+  for (u32 k = 0; k < it.ntile; ++k) {
+    if (k) __syncthreads();  // the previous tile's write-back has read shared memory
+    const u64 tile = (u64)it.tile + k;
+    if (J.C[pk] == 16) {
+      if (first)
+        pass_tile<16, true, INV, SCALE, true>(sm, in, out, n_in, s, l0, R, tab, t.cap, it.prime, tile);
+      else
+        pass_tile<16, false, INV, SCALE, true>(sm, in, out, n_in, s, l0, R, tab, t.cap, it.prime, tile);
+    } else {
+      if (first)
+        pass_tile<2, true, INV, SCALE, true>(sm, in, out, n_in, s, l0, R, tab, t.cap, it.prime, tile);
+      else
+        pass_tile<2, false, INV, SCALE, true>(sm, in, out, n_in, s, l0, R, tab, t.cap, it.prime, tile);
+    }
   }
 }
 
@@ -58,11 +61,18 @@ __global__ void __launch_bounds__(256, 3) batch_kernel(const BatchJob* __restric
                                                     u32* err, Tables t) {
   extern __shared__ u64 sm[];
   __shared__ u32 s_item;
+  // Thread 0 claims the next item while the current one runs, so the queue
+  // atomic's latency is hidden.  Items are claimed in queue order and depend
+  // only on earlier ones, so the earliest unfinished item is always being
+  // worked on: a claimed-but-waiting item never blocks its own dependencies.
+  u32 next = 0;
+  if (threadIdx.x == 0) next = atomicAdd(head, 1u);
   for (;;) {
-    if (threadIdx.x == 0) s_item = atomicAdd(head, 1u);
+    if (threadIdx.x == 0) s_item = next;
     __syncthreads();
     const u32 idx = s_item;
     if (idx >= n_items) break;
+    if (threadIdx.x == 0) next = atomicAdd(head, 1u);
     const BatchItem it = items[idx];
     const BatchJob& J = jobs[it.job];
     if (threadIdx.x == 0 && it.step > 0) {
@@ -90,11 +100,11 @@ __global__ void __launch_bounds__(256, 3) batch_kernel(const BatchJob* __restric
       }
       case kItemPointwise: {
         const u64 groups = L / 4;
-        const u64 g0 = (u64)it.tile * kPointwiseChunk;
+        const u64 g0 = (u64)it.tile * kBatchPointwiseChunk;
         const u64* a = J.res_a;
         const u64* b = J.square ? J.res_a : J.res_b;
         u64* d = J.square ? J.res_a : J.res_b;
-        for (u64 g = g0 + threadIdx.x; g < g0 + kPointwiseChunk && g < groups; g += blockDim.x)
+        for (u64 g = g0 + threadIdx.x; g < g0 + kBatchPointwiseChunk && g < groups; g += blockDim.x)
           pointwise_group<true>(d, a, b, L, t.root, t.cap, it.prime, g);
         break;
       }

@@ -344,7 +344,6 @@ nn_status scratch(nn_context* c, int slot, u64 words, u64** p) {
 // ---------------------------------------------------------------------------
 // Batches: a work queue over all jobs' pipeline steps (batch.cu).
 // ---------------------------------------------------------------------------
-constexpr u64 kPointwiseChunk = 1024;
 
 nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, const int* square, u64 count) {
   B->count = count;
@@ -409,7 +408,7 @@ nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, c
     for (u64 j = 0; j < count; ++j) {
       if (st >= steps[j]) continue;
       const nn::BatchJob& J = B->jobs[j];
-      auto push = [&](unsigned char kind, int pass, int prime, int operand, u64 tile) {
+      auto push = [&](unsigned char kind, int pass, int prime, int operand, u64 tile, u64 ntile = 1) {
         nn::BatchItem it{};
         it.job = (nn::u32)j;
         it.step = (unsigned short)st;
@@ -418,6 +417,7 @@ nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, c
         it.prime = (unsigned char)prime;
         it.operand = (unsigned char)operand;
         it.tile = (nn::u32)tile;
+        it.ntile = (unsigned short)ntile;
         B->items.push_back(it);
         B->need[J.ctr_base + st] += 1;
       };
@@ -428,19 +428,21 @@ nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, c
       const int m = J.n_pass;
       const u64 L = 1ull << J.s;
       if (st < m) {  // forward pass st of each operand
-        const u64 tiles = L / ((u64)J.C[st] << J.R[st]);
+        const u64 tw = (u64)J.C[st] << J.R[st], tiles = L / tw;
+        const u64 per = std::max<u64>(1, nn::kBatchItemWords / tw);
         for (int op = 0; op < (J.square ? 1 : 2); ++op)
           for (int pr = 0; pr < 3; ++pr)
-            for (u64 t = 0; t < tiles; ++t) push(nn::kItemFwd, st, pr, op, t);
+            for (u64 t = 0; t < tiles; t += per) push(nn::kItemFwd, st, pr, op, t, std::min(per, tiles - t));
       } else if (st == m) {
-        const u64 chunks = (L / 4 + kPointwiseChunk - 1) / kPointwiseChunk;
+        const u64 chunks = (L / 4 + nn::kBatchPointwiseChunk - 1) / nn::kBatchPointwiseChunk;
         for (int pr = 0; pr < 3; ++pr)
           for (u64 t = 0; t < chunks; ++t) push(nn::kItemPointwise, 0, pr, 0, t);
       } else if (st < 2 * m + 1) {  // inverse passes m-1 .. 0
         const int k = 2 * m - st;
-        const u64 tiles = L / ((u64)J.C[k] << J.R[k]);
+        const u64 tw = (u64)J.C[k] << J.R[k], tiles = L / tw;
+        const u64 per = std::max<u64>(1, nn::kBatchItemWords / tw);
         for (int pr = 0; pr < 3; ++pr)
-          for (u64 t = 0; t < tiles; ++t) push(nn::kItemInv, k, pr, 0, t);
+          for (u64 t = 0; t < tiles; t += per) push(nn::kItemInv, k, pr, 0, t, std::min(per, tiles - t));
       } else {
         for (u64 t = 0; t < nn::scan_tiles(J.na + J.nb); ++t) push(nn::kItemCrt, 0, 0, 0, t);
       }

@@ -58,7 +58,12 @@ constexpr int kScanThreads = 256;
 constexpr int kScanE = 8;  // limbs per thread
 constexpr u64 kScanTile = (u64)kScanThreads * kScanE;
 
-// Batched products (batch.cu): jobs, their work items, and the launch.
+// Batched products (batch.cu): jobs, their work items, and the launch.  A
+// pass item covers consecutive tiles worth at least kBatchItemWords residues
+// and a pointwise item kBatchPointwiseChunk groups of 4, so an item's fixed
+// cost (queue, dependency check, barriers) stays small beside its work.
+constexpr u64 kBatchItemWords = 8192;
+constexpr u64 kBatchPointwiseChunk = 4096;
 enum : unsigned char { kItemFwd = 0, kItemPointwise = 1, kItemInv = 2, kItemCrt = 3, kItemColumn = 4 };
 struct BatchJob {
   const u64* a;
@@ -78,7 +83,7 @@ struct BatchItem {
   u32 job;
   unsigned short step;
   unsigned char kind, pass, prime, operand;
-  unsigned short pad;
+  unsigned short ntile;  // consecutive tiles (pass items) handled by this item
   u32 tile;
 };
 cudaError_t batch_configure(int* blocks_per_sm, size_t smem);
