@@ -145,7 +145,9 @@ nn_status nn_batch_mul(nn_context* ctx, const nn_mul_job* jobs, uint64_t count);
 /* Tunables: "r_last" (levels of the contiguous NTT pass, 3..12, default 11),
  * "r_col" (most levels of a strided pass, 1..9, default 9), "r_last@<s>" and
  * "r_col@<s>" (the same for transforms of scale s only; 0 = default),
- * "batch_ntt_min" (default 384), "batch_blocks_per_sm" (0 = occupancy limit). */
+ * "batch_ntt_min" (default 384), "batch_blocks_per_sm" (0 = occupancy limit),
+ * "batch_item_words" (residues per prime a batch pass item covers at least,
+ * in consecutive tiles; default 8192). */
 nn_status nn_context_set_tunable(nn_context* ctx, const char* name, int64_t value);
 int64_t nn_context_get_tunable(const nn_context* ctx, const char* name);
 

@@ -79,30 +79,37 @@ def tune_passes(ctx, n_exps) -> tuple[dict, dict]:
 
 
 def tune_batch(ctx, jobs: int) -> tuple[dict, dict]:
+    """CTAs per SM, the shortest operand sent down the NTT route, and the
+    residues per pass item, on an uneven workload of `jobs` products; every
+    setting must give the same products."""
     import torch
 
     from .workloads import UnevenProducts
     W = UnevenProducts(jobs, seed=5)
     results = {}
     ref = None
-    for per_sm in (1, 2, 3):
-        for ntt_min in (128, 256, 384, 768):
-            ctx.set_tunable("batch_blocks_per_sm", per_sm)
-            ctx.set_tunable("batch_ntt_min", ntt_min)
-            plan = ctx.batch(W.sa, W.sb)
-            ms = _time(lambda: plan.run_jobs(W.jobs_batch), 3)
-            ctx.synchronize()
-            if ref is None:
-                ref = W.out_batch.clone()
-            elif not torch.equal(ref, W.out_batch):
-                raise RuntimeError(f"per_sm={per_sm} ntt_min={ntt_min} changed a product")
-            plan.close()
-            results[f"{per_sm},{ntt_min}"] = ms
+    for per_sm in (2, 3):
+        for ntt_min in (128, 256, 384):
+            for item in (4096, 8192, 16384, 32768):
+                ctx.set_tunable("batch_blocks_per_sm", per_sm)
+                ctx.set_tunable("batch_ntt_min", ntt_min)
+                ctx.set_tunable("batch_item_words", item)
+                plan = ctx.batch(W.sa, W.sb)
+                ms = _time(lambda: plan.run_jobs(W.jobs_batch), 3)
+                ctx.synchronize()
+                if ref is None:
+                    ref = W.out_batch.clone()
+                elif not torch.equal(ref, W.out_batch):
+                    raise RuntimeError(f"per_sm={per_sm} ntt_min={ntt_min} item={item} changed a product")
+                plan.close()
+                results[f"{per_sm},{ntt_min},{item}"] = ms
     best = min(results, key=results.get)
-    per_sm, ntt_min = map(int, best.split(","))
+    per_sm, ntt_min, item = map(int, best.split(","))
     ctx.set_tunable("batch_blocks_per_sm", per_sm)
     ctx.set_tunable("batch_ntt_min", ntt_min)
-    return {"batch_blocks_per_sm": per_sm, "batch_ntt_min": ntt_min}, {"batch_%d_ms" % jobs: results}
+    ctx.set_tunable("batch_item_words", item)
+    return ({"batch_blocks_per_sm": per_sm, "batch_ntt_min": ntt_min, "batch_item_words": item},
+            {"batch_%d_ms" % jobs: results})
 
 
 def main() -> None:

@@ -54,6 +54,7 @@ struct nn_context {
     return nn::plan_passes(s, rl, rc);
   }
   u64 batch_ntt_min = 384;    // batches: schoolbook when min(n_a, n_b) is below this
+  u64 batch_item_words = nn::kBatchItemWords;  // residues a pass item covers at least
   int batch_blocks_per_sm = 0;  // persistent CTAs per SM (0: occupancy limit)
 };
 
@@ -429,7 +430,7 @@ nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, c
       const u64 L = 1ull << J.s;
       if (st < m) {  // forward pass st of each operand
         const u64 tw = (u64)J.C[st] << J.R[st], tiles = L / tw;
-        const u64 per = std::max<u64>(1, nn::kBatchItemWords / tw);
+        const u64 per = std::max<u64>(1, c->batch_item_words / tw);
         for (int op = 0; op < (J.square ? 1 : 2); ++op)
           for (int pr = 0; pr < 3; ++pr)
             for (u64 t = 0; t < tiles; t += per) push(nn::kItemFwd, st, pr, op, t, std::min(per, tiles - t));
@@ -440,7 +441,7 @@ nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, c
       } else if (st < 2 * m + 1) {  // inverse passes m-1 .. 0
         const int k = 2 * m - st;
         const u64 tw = (u64)J.C[k] << J.R[k], tiles = L / tw;
-        const u64 per = std::max<u64>(1, nn::kBatchItemWords / tw);
+        const u64 per = std::max<u64>(1, c->batch_item_words / tw);
         for (int pr = 0; pr < 3; ++pr)
           for (u64 t = 0; t < tiles; t += per) push(nn::kItemInv, k, pr, 0, t, std::min(per, tiles - t));
       } else {
@@ -891,6 +892,8 @@ nn_status nn_context_set_tunable(nn_context* c, const char* name, int64_t v) {
     c->r_col = (int)v;
   else if (k == "batch_ntt_min" && v >= 1)
     c->batch_ntt_min = (u64)v;
+  else if (k == "batch_item_words" && v >= 1 && v <= (1 << 20))
+    c->batch_item_words = (u64)v;
   else if (k == "batch_blocks_per_sm" && v >= 0 && v <= 32)
     c->batch_blocks_per_sm = (int)v;
   else {
@@ -914,6 +917,7 @@ int64_t nn_context_get_tunable(const nn_context* c, const char* name) {
   if (k == "r_last") return c->r_last;
   if (k == "r_col") return c->r_col;
   if (k == "batch_ntt_min") return (int64_t)c->batch_ntt_min;
+  if (k == "batch_item_words") return (int64_t)c->batch_item_words;
   if (k == "batch_blocks_per_sm") return c->batch_blocks_per_sm;
   return -1;
 }
