@@ -147,7 +147,12 @@ nn_status nn_batch_mul(nn_context* ctx, const nn_mul_job* jobs, uint64_t count);
  * "r_col@<s>" (the same for transforms of scale s only; 0 = default),
  * "batch_ntt_min" (default 384), "batch_blocks_per_sm" (0 = occupancy limit),
  * "batch_item_words" (residues per prime a batch pass item covers at least,
- * in consecutive tiles; default 8192). */
+ * in consecutive tiles; default 8192), "batch_fused" (1, the default: a
+ * batched transform of two passes or more runs the second operand's last
+ * forward pass, the pointwise product and the first inverse pass as one
+ * step; 0: as separate steps), "batch_merge" (1, the default: a batched
+ * pass whose tiles hold fewer than 2048 words works on several of them as one
+ * tile; 0: tile by tile). */
 nn_status nn_context_set_tunable(nn_context* ctx, const char* name, int64_t value);
 int64_t nn_context_get_tunable(const nn_context* ctx, const char* name);
 

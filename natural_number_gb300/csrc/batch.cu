@@ -4,7 +4,10 @@
 // job with a short pipeline of steps — for an NTT job at scale s: the forward
 // passes of both operands (step k = pass k), the pointwise product, the
 // inverse passes, the CRT + carry scan; for a short operand (schoolbook job):
-// one column-sum scan — and every step is cut into tiles (items).  Items are
+// one column-sum scan — and every step is cut into tiles (items).  When the
+// transform has two passes or more, the second operand's last forward pass,
+// the pointwise product and the first inverse pass are one step (fused
+// items), after the first operand's last pass.  Items are
 // sorted by step, then job, then tile.  A fixed grid of CTAs (all resident)
 // pulls items from an atomic head; an item of step k of job j waits until all
 // items of step k-1 of job j have completed (a per-(job, step) counter).
@@ -32,26 +35,55 @@ __device__ __forceinline__ u32 ld_acquire(const u32* p) {
   return v;
 }
 
+// Wide strided tiles (32, 64 or 128 columns) of a transform's first pass:
+// the forward pass that loads limbs, or the last inverse pass, which scales.
+template <bool INV>
+__device__ __forceinline__ void wide_tile(int C, u64* sm, const u64* in, u64* out, u64 n_in, int s, int l0, int R,
+                                          const u64* tab, const Tables& t, int prime, u64 tile) {
+  if (C == 32)
+    pass_tile<32, !INV, INV, INV, true>(sm, in, out, n_in, s, l0, R, tab, t.cap, prime, tile);
+  else if (C == 64)
+    pass_tile<64, !INV, INV, INV, true>(sm, in, out, n_in, s, l0, R, tab, t.cap, prime, tile);
+  else
+    pass_tile<128, !INV, INV, INV, true>(sm, in, out, n_in, s, l0, R, tab, t.cap, prime, tile);
+}
+
 template <bool INV, bool SCALE>
 __device__ __forceinline__ void run_pass(u64* sm, const BatchJob& J, const BatchItem& it, const u64* in, u64* out,
                                          u64 n_in, const Tables& t, bool first) {
   const int pk = it.pass;
-  const int s = J.s, l0 = J.lambda0[pk], R = J.R[pk];
+  const int s = J.s, l0 = J.lambda0[pk], R = J.R[pk], C = J.C[pk], skip = J.skip[pk];
   const u64* tab = INV ? t.iroot : t.root;
   for (u32 k = 0; k < it.ntile; ++k) {
     if (k) __syncthreads();  // the previous tile's write-back has read shared memory
     const u64 tile = (u64)it.tile + k;
-    if (J.C[pk] == 16) {
+    if (C == 16) {
       if (first)
         pass_tile<16, true, INV, SCALE, true>(sm, in, out, n_in, s, l0, R, tab, t.cap, it.prime, tile);
       else
         pass_tile<16, false, INV, SCALE, true>(sm, in, out, n_in, s, l0, R, tab, t.cap, it.prime, tile);
-    } else {
+    } else if (C == 2) {
       if (first)
         pass_tile<2, true, INV, SCALE, true>(sm, in, out, n_in, s, l0, R, tab, t.cap, it.prime, tile);
       else
-        pass_tile<2, false, INV, SCALE, true>(sm, in, out, n_in, s, l0, R, tab, t.cap, it.prime, tile);
+        pass_tile<2, false, INV, SCALE, true>(sm, in, out, n_in, s, l0, R, tab, t.cap, it.prime, tile, nullptr,
+                                              nullptr, skip);
+    } else if constexpr (INV == SCALE) {  // the planner widens pass 0 only
+      wide_tile<INV>(C, sm, in, out, n_in, s, l0, R, tab, t, it.prime, tile);
     }
+  }
+}
+
+// The last forward pass of the second operand (or of the only one, for a
+// square), the pointwise product with the first operand's finished residues
+// and the first inverse pass, tile by tile (the contiguous pass only).
+__device__ __forceinline__ void run_fused(u64* sm, const BatchJob& J, const BatchItem& it, u64* r, const u64* other,
+                                          const Tables& t) {
+  const int pk = it.pass;
+  for (u32 k = 0; k < it.ntile; ++k) {
+    if (k) __syncthreads();
+    pass_tile<2, false, false, false, true, true>(sm, r, r, 0, J.s, J.lambda0[pk], J.R[pk], t.root, t.cap, it.prime,
+                                                  (u64)it.tile + k, t.iroot, other, J.skip[pk]);
   }
 }
 
@@ -116,6 +148,9 @@ __global__ void __launch_bounds__(256, 3) batch_kernel(const BatchJob* __restric
           run_pass<true, false>(sm, J, it, r, r, 0, t, false);
         break;
       }
+      case kItemFused:
+        run_fused(sm, J, it, J.square ? J.res_a : J.res_b, J.square ? nullptr : J.res_a, t);
+        break;
       case kItemCrt: {
         const u64 size = J.na + J.nb;
         CrtProducerT<true> prod{J.square ? J.res_a : J.res_b, L, size - 1};

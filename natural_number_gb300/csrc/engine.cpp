@@ -21,6 +21,7 @@ using nn::u64;
 
 namespace {
 constexpr u64 kNttMulThreshold = 384;  // ntt_info.h:6
+constexpr int kMergedTileWords = 2048;  // batch tiles: 256 threads x radix-8 units
 
 int ntt_scale(u64 n1, u64 n2) {  // get_NTT_scale (natural.h:384-386)
   u64 v = n1 + n2 - 2;
@@ -55,6 +56,8 @@ struct nn_context {
   }
   u64 batch_ntt_min = 384;    // batches: schoolbook when min(n_a, n_b) is below this
   u64 batch_item_words = nn::kBatchItemWords;  // residues a pass item covers at least
+  int batch_fused = 1;        // batches: fused last pass (forward + pointwise + inverse)
+  int batch_merge = 1;        // batches: small tiles worked on 2048 words at a time
   int batch_blocks_per_sm = 0;  // persistent CTAs per SM (0: occupancy limit)
 };
 
@@ -354,6 +357,7 @@ nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, c
   B->off_a.assign(count, 0);
   B->off_b.assign(count, 0);
   std::vector<int> steps(count, 0);
+  std::vector<int> fused_at(count, -1);  // step of the fused items, -1 without
   int max_s = 2;
   size_t smem = 8;
   for (u64 j = 0; j < count; ++j) {
@@ -390,9 +394,34 @@ nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, c
         J.lambda0[k] = plan[k].lambda0;
         J.R[k] = plan[k].R;
         J.C[k] = plan[k].C;
-        smem = std::max(smem, nn::tile_smem_bytes(plan[k].C, plan[k].R));
+        J.skip[k] = 0;
+        if (c->batch_merge) {
+          // Small tiles leave most of a CTA's 256 threads idle and cut the
+          // levels into radix-2 and radix-4 sweeps; work on 2048 words at once:
+          // pass 0's strided tiles get up to 128 columns (as many as its
+          // column blocks hold), later contiguous passes take 2^skip
+          // consecutive tiles as one tile of R + skip levels.
+          const int lg_s = s - plan[k].lambda0 - plan[k].R;
+          if (k == 0 && plan[k].C == 16)
+            while ((J.C[k] << J.R[k]) < kMergedTileWords && J.C[k] < 128 && 2 * J.C[k] <= (1 << lg_s)) J.C[k] *= 2;
+          if (k > 0 && plan[k].C == 2)
+            while ((2 << J.R[k]) < kMergedTileWords && J.skip[k] < plan[k].lambda0) {
+              ++J.skip[k];
+              ++J.R[k];
+              --J.lambda0[k];
+            }
+        }
+        smem = std::max(smem, nn::tile_smem_bytes(J.C[k], J.R[k]));
       }
-      steps[j] = 2 * J.n_pass + 2;
+      const int m = J.n_pass;
+      if (c->batch_fused && m >= 2 && J.C[m - 1] == 2) {
+        // forward passes 0..m-2 of both operands, the first operand's last
+        // pass (not for a square), the fused step, inverse passes m-2..0, CRT
+        fused_at[j] = J.square ? m - 1 : m;
+        steps[j] = fused_at[j] + m + 1;
+      } else {
+        steps[j] = 2 * m + 2;
+      }
       B->off_a[j] = B->arena_words;
       B->arena_words += 3ull << s;
       if (!J.square) {
@@ -428,6 +457,26 @@ nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, c
       }
       const int m = J.n_pass;
       const u64 L = 1ull << J.s;
+      auto pass_items = [&](unsigned char kind, int k, int operand) {
+        const u64 tw = (u64)J.C[k] << J.R[k], tiles = L / tw;
+        const u64 per = std::max<u64>(1, c->batch_item_words / tw);
+        for (int pr = 0; pr < 3; ++pr)
+          for (u64 t = 0; t < tiles; t += per) push(kind, k, pr, operand, t, std::min(per, tiles - t));
+      };
+      if (const int f = fused_at[j]; f >= 0) {
+        if (st < m - 1) {
+          for (int op = 0; op < (J.square ? 1 : 2); ++op) pass_items(nn::kItemFwd, st, op);
+        } else if (st < f) {
+          pass_items(nn::kItemFwd, m - 1, 0);  // the first operand's last pass
+        } else if (st == f) {
+          pass_items(nn::kItemFused, m - 1, 0);
+        } else if (st < f + m) {
+          pass_items(nn::kItemInv, f + m - 1 - st, 0);  // inverse passes m-2 .. 0
+        } else {
+          for (u64 t = 0; t < nn::scan_tiles(J.na + J.nb); ++t) push(nn::kItemCrt, 0, 0, 0, t);
+        }
+        continue;
+      }
       if (st < m) {  // forward pass st of each operand
         const u64 tw = (u64)J.C[st] << J.R[st], tiles = L / tw;
         const u64 per = std::max<u64>(1, c->batch_item_words / tw);
@@ -894,6 +943,10 @@ nn_status nn_context_set_tunable(nn_context* c, const char* name, int64_t v) {
     c->batch_ntt_min = (u64)v;
   else if (k == "batch_item_words" && v >= 1 && v <= (1 << 20))
     c->batch_item_words = (u64)v;
+  else if (k == "batch_fused" && (v == 0 || v == 1))
+    c->batch_fused = (int)v;
+  else if (k == "batch_merge" && (v == 0 || v == 1))
+    c->batch_merge = (int)v;
   else if (k == "batch_blocks_per_sm" && v >= 0 && v <= 32)
     c->batch_blocks_per_sm = (int)v;
   else {
@@ -918,6 +971,8 @@ int64_t nn_context_get_tunable(const nn_context* c, const char* name) {
   if (k == "r_col") return c->r_col;
   if (k == "batch_ntt_min") return (int64_t)c->batch_ntt_min;
   if (k == "batch_item_words") return (int64_t)c->batch_item_words;
+  if (k == "batch_fused") return (int64_t)c->batch_fused;
+  if (k == "batch_merge") return (int64_t)c->batch_merge;
   if (k == "batch_blocks_per_sm") return c->batch_blocks_per_sm;
   return -1;
 }

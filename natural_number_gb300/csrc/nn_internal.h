@@ -64,7 +64,7 @@ constexpr u64 kScanTile = (u64)kScanThreads * kScanE;
 // cost (queue, dependency check, barriers) stays small beside its work.
 constexpr u64 kBatchItemWords = 8192;
 constexpr u64 kBatchPointwiseChunk = 4096;
-enum : unsigned char { kItemFwd = 0, kItemPointwise = 1, kItemInv = 2, kItemCrt = 3, kItemColumn = 4 };
+enum : unsigned char { kItemFwd = 0, kItemPointwise = 1, kItemInv = 2, kItemCrt = 3, kItemColumn = 4, kItemFused = 5 };
 struct BatchJob {
   const u64* a;
   const u64* b;
@@ -77,7 +77,10 @@ struct BatchJob {
   int s;         // transform scale; 0 for a schoolbook job
   int square;    // a == b: one transform
   int n_pass;
-  int lambda0[4], R[4], C[4];
+  // Pass k covers levels [lambda0 + skip, lambda0 + R) in tiles of C columns x
+  // 2^R rows: the batch widens pass 0's strided tiles (C up to 128) and runs
+  // later contiguous passes in tiles of 2^skip consecutive tiles.
+  int lambda0[4], R[4], C[4], skip[4];
 };
 struct BatchItem {
   u32 job;

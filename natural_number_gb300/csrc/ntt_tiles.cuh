@@ -219,13 +219,13 @@ __device__ __forceinline__ void tile_forward(u64* sm, int R, u64 ksb, const u64*
   }
 }
 
-// Inverse levels R-1 .. 0 of the tile in shared memory.
+// Inverse levels R-1 .. l_stop of the tile in shared memory.
 template <int C, int PR>
-__device__ __forceinline__ void tile_inverse(u64* sm, int R, u64 ksb, const u64* tw, const u64* tws) {
+__device__ __forceinline__ void tile_inverse(u64* sm, int R, u64 ksb, const u64* tw, const u64* tws, int l_stop = 0) {
   const int cap = group_cap(C, R);
-  const int n = (R + cap - 1) / cap;
+  const int n = (R - l_stop + cap - 1) / cap;
   for (int g = 0, l = R; g < n; ++g) {
-    const int k = (l + (n - g) - 1) / (n - g);
+    const int k = (l - l_stop + (n - g) - 1) / (n - g);
     l -= k;
     run_group<C, true, PR>(sm, k, l, R, ksb, tw, tws);
     __syncthreads();
@@ -256,10 +256,13 @@ __device__ __forceinline__ void pointwise4(u64 (&o)[4], const u64 (&A)[4], const
 // FUSED (contiguous passes only): after the forward levels, multiply
 // pointwise by the other operand's residues `other` and run the inverse
 // levels before writing back.
+// skip: the first `skip` local levels are not run (already done by the pass
+// before).  A contiguous tile of R levels with skip = w is 2^w consecutive
+// tiles of R - w levels, so small tiles can be worked on together.
 template <int C, bool FIRST, bool INV, bool SCALE, bool CG, bool FUSED, int PR>
 __device__ __forceinline__ void pass_tile_p(u64* sm, const u64* in, u64* out, u64 n_in, int s, int lambda0, int R,
                                             const u64* __restrict__ tab, const u64* __restrict__ itab, u64 tab_stride,
-                                            u64 tile, const u64* other) {
+                                            u64 tile, const u64* other, int skip) {
   constexpr u64 p = PrimeC<PR>::p;
   constexpr u32 ch = PrimeC<PR>::c_hi;
   const u64 L = 1ull << s;
@@ -269,7 +272,8 @@ __device__ __forceinline__ void pass_tile_p(u64* sm, const u64* in, u64* out, u6
   const u64 ksb = tile / tiles_per_sb;
   const u64 base = (ksb << (lg_s + R)) + (tile % tiles_per_sb) * C;
   const u32 nel = (u32)C << R;
-  constexpr int LGC = C == 16 ? 4 : 1;
+  static_assert(C == 2 || C == 16 || C == 32 || C == 64 || C == 128, "tile widths");
+  constexpr int LGC = C == 2 ? 1 : C == 16 ? 4 : C == 32 ? 5 : C == 64 ? 6 : 7;
 
   // With every limb in the lower half of the transform (n_in <= L/2), level 0
   // pairs each limb with a zero: both outputs are the limb's residue, written
@@ -311,7 +315,7 @@ __device__ __forceinline__ void pass_tile_p(u64* sm, const u64* in, u64* out, u6
   __syncthreads();
 
   if (!INV) {
-    tile_forward<C, PR>(sm, R, ksb, tw, tws, half ? 1 : 0);
+    tile_forward<C, PR>(sm, R, ksb, tw, tws, half ? 1 : skip);
     if (FUSED) {  // contiguous tile: smem index == position - base; other == nullptr squares
       const u64* oth = other ? other + (u64)PR * L : nullptr;
       const ulonglong2* twsv = reinterpret_cast<const ulonglong2*>(tws);
@@ -336,10 +340,10 @@ __device__ __forceinline__ void pass_tile_p(u64* sm, const u64* in, u64* out, u6
       stage_twiddles(tws, itw, ksb, R);
       cp_async_wait_all();
       __syncthreads();
-      tile_inverse<C, PR>(sm, R, ksb, itw, tws);
+      tile_inverse<C, PR>(sm, R, ksb, itw, tws, skip);
     }
   } else {
-    tile_inverse<C, PR>(sm, R, ksb, tw, tws);
+    tile_inverse<C, PR>(sm, R, ksb, tw, tws, skip);
   }
 
   u64* dst = out + (u64)PR * L;
@@ -357,16 +361,17 @@ __device__ __forceinline__ void pass_tile_p(u64* sm, const u64* in, u64* out, u6
 template <int C, bool FIRST, bool INV, bool SCALE, bool CG, bool FUSED = false>
 __device__ __forceinline__ void pass_tile(u64* sm, const u64* in, u64* out, u64 n_in, int s, int lambda0, int R,
                                           const u64* __restrict__ tab, u64 tab_stride, int prime, u64 tile,
-                                          const u64* __restrict__ itab = nullptr, const u64* other = nullptr) {
+                                          const u64* __restrict__ itab = nullptr, const u64* other = nullptr,
+                                          int skip = 0) {
   if (prime == 0)
     pass_tile_p<C, FIRST, INV, SCALE, CG, FUSED, 0>(sm, in, out, n_in, s, lambda0, R, tab, itab, tab_stride, tile,
-                                                   other);
+                                                   other, skip);
   else if (prime == 1)
     pass_tile_p<C, FIRST, INV, SCALE, CG, FUSED, 1>(sm, in, out, n_in, s, lambda0, R, tab, itab, tab_stride, tile,
-                                                   other);
+                                                   other, skip);
   else
     pass_tile_p<C, FIRST, INV, SCALE, CG, FUSED, 2>(sm, in, out, n_in, s, lambda0, R, tab, itab, tab_stride, tile,
-                                                   other);
+                                                   other, skip);
 }
 
 // Pointwise product of one group g (4 residues) of prime i.

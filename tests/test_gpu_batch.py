@@ -74,3 +74,57 @@ def test_batch_squares_and_threshold_tunable(ctx, oracle):
             assert np.array_equal(normalize(outs[k]), oracle.mul(a_list[k], b_list[k]))
     finally:
         ctx.set_tunable("batch_ntt_min", old)
+
+
+def test_batch_fused_last_pass_matches_unfused(ctx, oracle):
+    """The fused step (second operand's last forward pass + pointwise + first
+    inverse pass) and the separate steps give the same products, for two- and
+    three-pass transforms, products and squares."""
+    sizes = [(384, 384), (1000, 3000), (4096, 4096), (20000, 20001), (70000, 1000), (200000, 300000),
+             (1200000, 1100000), (5000, 5000), (300000, 300000)]
+    square = [0] * 7 + [1, 1]
+    a_list = [limbs(k + 301, x) for k, (x, _) in enumerate(sizes)]
+    b_list = [a_list[k] if square[k] else limbs(k + 401, y) for k, (_, y) in enumerate(sizes)]
+    old = ctx.get_tunable("batch_fused")
+    try:
+        ctx.set_tunable("batch_fused", 0)
+        plain, p0 = run_batch(ctx, a_list, b_list, square=square)
+        ctx.set_tunable("batch_fused", 1)
+        fused, p1 = run_batch(ctx, a_list, b_list, square=square)
+    finally:
+        ctx.set_tunable("batch_fused", old)
+    assert p1.items < p0.items  # the pointwise and first inverse items are gone
+    for k in range(len(sizes)):
+        assert np.array_equal(fused[k], plain[k]), k
+        want = oracle.sqr(a_list[k]) if square[k] else oracle.mul(a_list[k], b_list[k])
+        assert np.array_equal(normalize(fused[k]), want), k
+
+
+def test_batch_merged_tiles_match_unmerged(ctx, oracle):
+    """Widened strided tiles and merged contiguous tiles (transforms of scale
+    13-18, where the passes' own tiles hold 32-1024 words) give the same
+    products as tile-by-tile work, and the oracle's."""
+    sizes = [(2000, 2100), (3000, 3000), (6000, 5000), (10000, 12000), (30000, 30000), (60000, 60000),
+             (100000, 100000), (65536, 500), (20000, 20000), (4000, 4000)]
+    square = [0] * 8 + [1, 1]
+    a_list = [limbs(k + 501, x) for k, (x, _) in enumerate(sizes)]
+    b_list = [a_list[k] if square[k] else limbs(k + 601, y) for k, (_, y) in enumerate(sizes)]
+    old = ctx.get_tunable("batch_merge")
+    old_rl = {s: ctx.get_tunable("r_last@%d" % s) for s in (13, 16)}
+    try:
+        ctx.set_tunable("batch_merge", 0)
+        plain, _ = run_batch(ctx, a_list, b_list, square=square)
+        ctx.set_tunable("batch_merge", 1)
+        merged, _ = run_batch(ctx, a_list, b_list, square=square)
+        ctx.set_tunable("r_last@13", 6)  # a 6-level strided pass widened to 32 columns
+        ctx.set_tunable("r_last@16", 7)
+        merged2, _ = run_batch(ctx, a_list, b_list, square=square)
+    finally:
+        ctx.set_tunable("batch_merge", old)
+        for s, v in old_rl.items():
+            ctx.set_tunable("r_last@%d" % s, v)
+    for k in range(len(sizes)):
+        want = oracle.sqr(a_list[k]) if square[k] else oracle.mul(a_list[k], b_list[k])
+        assert np.array_equal(normalize(plain[k]), want), k
+        assert np.array_equal(merged[k], plain[k]), k
+        assert np.array_equal(merged2[k], plain[k]), k
