@@ -152,7 +152,10 @@ nn_status nn_batch_mul(nn_context* ctx, const nn_mul_job* jobs, uint64_t count);
  * forward pass, the pointwise product and the first inverse pass as one
  * step; 0: as separate steps), "batch_merge" (1, the default: a batched
  * pass whose tiles hold fewer than 2048 words works on several of them as one
- * tile; 0: tile by tile). */
+ * tile; 0: tile by tile), "batch_split" (1, the default: an unbalanced
+ * product may run as pieces of its longer operand, each through a smaller
+ * transform sharing the shorter operand's, when that is estimated faster;
+ * 0: one transform per product). */
 nn_status nn_context_set_tunable(nn_context* ctx, const char* name, int64_t value);
 int64_t nn_context_get_tunable(const nn_context* ctx, const char* name);
 

@@ -5,9 +5,12 @@
 // passes of both operands (step k = pass k), the pointwise product, the
 // inverse passes, the CRT + carry scan; for a short operand (schoolbook job):
 // one column-sum scan — and every step is cut into tiles (items).  When the
-// transform has two passes or more, the second operand's last forward pass,
+// transform has two passes or more, the first operand's last forward pass,
 // the pointwise product and the first inverse pass are one step (fused
-// items), after the first operand's last pass.  Items are
+// items), after the second operand's last pass.  An unbalanced product may
+// be split: the longer operand (operand 0) in pieces, each with its own
+// transform, sharing the shorter operand's; the CRT + carry scan sums the
+// pieces' overlapping coefficients.  Items are
 // sorted by step, then job, then tile.  A fixed grid of CTAs (all resident)
 // pulls items from an atomic head; an item of step k of job j waits until all
 // items of step k-1 of job j have completed (a per-(job, step) counter).
@@ -48,15 +51,45 @@ __device__ __forceinline__ void wide_tile(int C, u64* sm, const u64* in, u64* ou
     pass_tile<128, !INV, INV, INV, true>(sm, in, out, n_in, s, l0, R, tab, t.cap, prime, tile);
 }
 
+// The transform that tile g of a pass over the first operand's pieces
+// belongs to, and the tile's index within it.
+struct PieceTile {
+  u64 piece, tile;
+};
+__device__ __forceinline__ PieceTile piece_tile(const BatchJob& J, u64 g, u64 tiles_per_transform) {
+  if (J.pieces == 1) return {0, g};
+  const u64 i = g / tiles_per_transform;
+  return {i, g - i * tiles_per_transform};
+}
+
+// One pass item: forward passes of operand 0 (the pieces of the longer
+// operand) or 1 (the shorter), inverse passes of operand 0.
 template <bool INV, bool SCALE>
-__device__ __forceinline__ void run_pass(u64* sm, const BatchJob& J, const BatchItem& it, const u64* in, u64* out,
-                                         u64 n_in, const Tables& t, bool first) {
+__device__ __forceinline__ void run_pass(u64* sm, const BatchJob& J, const BatchItem& it, int operand,
+                                         const Tables& t, bool first) {
   const int pk = it.pass;
   const int s = J.s, l0 = J.lambda0[pk], R = J.R[pk], C = J.C[pk], skip = J.skip[pk];
+  const u64 L = 1ull << s;
   const u64* tab = INV ? t.iroot : t.root;
   for (u32 k = 0; k < it.ntile; ++k) {
     if (k) __syncthreads();  // the previous tile's write-back has read shared memory
-    const u64 tile = (u64)it.tile + k;
+    const u64* in;
+    u64* out;
+    u64 n_in = 0, tile = (u64)it.tile + k;
+    if (operand == 0) {
+      const PieceTile pt = piece_tile(J, tile, L / ((u64)C << R));
+      tile = pt.tile;
+      out = J.res_a + pt.piece * 3 * L;
+      in = out;
+      if (first) {
+        in = J.a + pt.piece * J.piece;
+        n_in = min(J.piece, J.na - pt.piece * J.piece);
+      }
+    } else {
+      out = J.res_b;
+      in = first ? J.b : out;
+      n_in = J.nb;
+    }
     if (C == 16) {
       if (first)
         pass_tile<16, true, INV, SCALE, true>(sm, in, out, n_in, s, l0, R, tab, t.cap, it.prime, tile);
@@ -74,16 +107,20 @@ __device__ __forceinline__ void run_pass(u64* sm, const BatchJob& J, const Batch
   }
 }
 
-// The last forward pass of the second operand (or of the only one, for a
-// square), the pointwise product with the first operand's finished residues
-// and the first inverse pass, tile by tile (the contiguous pass only).
-__device__ __forceinline__ void run_fused(u64* sm, const BatchJob& J, const BatchItem& it, u64* r, const u64* other,
-                                          const Tables& t) {
+// The last forward pass of the first operand's pieces (or of the only
+// operand, for a square), the pointwise product with the second operand's
+// finished residues and the first inverse pass, tile by tile (the contiguous
+// pass only).
+__device__ __forceinline__ void run_fused(u64* sm, const BatchJob& J, const BatchItem& it, const Tables& t) {
   const int pk = it.pass;
+  const u64 L = 1ull << J.s;
+  const u64* other = J.square ? nullptr : J.res_b;
   for (u32 k = 0; k < it.ntile; ++k) {
     if (k) __syncthreads();
+    const PieceTile pt = piece_tile(J, (u64)it.tile + k, L / (2ull << J.R[pk]));
+    u64* r = J.res_a + pt.piece * 3 * L;
     pass_tile<2, false, false, false, true, true>(sm, r, r, 0, J.s, J.lambda0[pk], J.R[pk], t.root, t.cap, it.prime,
-                                                  (u64)it.tile + k, t.iroot, other, J.skip[pk]);
+                                                  pt.tile, t.iroot, other, J.skip[pk]);
   }
 }
 
@@ -123,38 +160,38 @@ __global__ void __launch_bounds__(256, 3) batch_kernel(const BatchJob* __restric
     __syncthreads();
     const u64 L = 1ull << J.s;
     switch (it.kind) {
-      case kItemFwd: {
-        const bool first = it.pass == 0;
-        const u64* src = first ? (it.operand ? J.b : J.a) : (it.operand ? J.res_b : J.res_a);
-        u64* dst = it.operand ? J.res_b : J.res_a;
-        run_pass<false, false>(sm, J, it, src, dst, it.operand ? J.nb : J.na, t, first);
+      case kItemFwd:
+        run_pass<false, false>(sm, J, it, it.operand, t, it.pass == 0);
         break;
-      }
-      case kItemPointwise: {
+      case kItemPointwise: {  // piece i's residues times the other operand's, in place
         const u64 groups = L / 4;
-        const u64 g0 = (u64)it.tile * kBatchPointwiseChunk;
-        const u64* a = J.res_a;
-        const u64* b = J.square ? J.res_a : J.res_b;
-        u64* d = J.square ? J.res_a : J.res_b;
+        const u64 chunks = (groups + kBatchPointwiseChunk - 1) / kBatchPointwiseChunk;
+        const PieceTile pt = piece_tile(J, it.tile, chunks);
+        const u64 g0 = pt.tile * kBatchPointwiseChunk;
+        u64* d = J.res_a + pt.piece * 3 * L;
+        const u64* b = J.square ? d : J.res_b;
         for (u64 g = g0 + threadIdx.x; g < g0 + kBatchPointwiseChunk && g < groups; g += blockDim.x)
-          pointwise_group<true>(d, a, b, L, t.root, t.cap, it.prime, g);
+          pointwise_group<true>(d, d, b, L, t.root, t.cap, it.prime, g);
         break;
       }
-      case kItemInv: {
-        u64* r = J.square ? J.res_a : J.res_b;
+      case kItemInv:
         if (it.pass == 0)
-          run_pass<true, true>(sm, J, it, r, r, 0, t, false);
+          run_pass<true, true>(sm, J, it, 0, t, false);
         else
-          run_pass<true, false>(sm, J, it, r, r, 0, t, false);
+          run_pass<true, false>(sm, J, it, 0, t, false);
         break;
-      }
       case kItemFused:
-        run_fused(sm, J, it, J.square ? J.res_a : J.res_b, J.square ? nullptr : J.res_a, t);
+        run_fused(sm, J, it, t);
         break;
       case kItemCrt: {
         const u64 size = J.na + J.nb;
-        CrtProducerT<true> prod{J.square ? J.res_a : J.res_b, L, size - 1};
-        scan_tile(prod, it.tile, size, J.out, size, nullptr, flags + J.flag_base, err);
+        if (J.pieces == 1) {
+          CrtProducerT<true> prod{J.res_a, L, size - 1};
+          scan_tile(prod, it.tile, size, J.out, size, nullptr, flags + J.flag_base, err);
+        } else {
+          PieceCrtProducer prod{J.res_a, L, J.piece, J.pieces, J.nb, size - 1};
+          scan_tile(prod, it.tile, size, J.out, size, nullptr, flags + J.flag_base, err);
+        }
         break;
       }
       case kItemColumn: {

@@ -58,6 +58,7 @@ struct nn_context {
   u64 batch_item_words = nn::kBatchItemWords;  // residues a pass item covers at least
   int batch_fused = 1;        // batches: fused last pass (forward + pointwise + inverse)
   int batch_merge = 1;        // batches: small tiles worked on 2048 words at a time
+  int batch_split = 1;        // batches: unbalanced products in pieces sharing one transform
   int batch_blocks_per_sm = 0;  // persistent CTAs per SM (0: occupancy limit)
 };
 
@@ -68,6 +69,7 @@ struct nn_batch {
   std::vector<nn::BatchItem> items;
   std::vector<nn::u32> need;
   std::vector<u64> off_a, off_b;
+  std::vector<char> swap;  // NTT job whose second operand is the longer one
   u64 arena_words = 0;
   nn::u32 n_ctrs = 0, n_flags = 0;
   size_t smem = 0;
@@ -349,6 +351,45 @@ nn_status scratch(nn_context* c, int slot, u64 words, u64** p) {
 // Batches: a work queue over all jobs' pipeline steps (batch.cu).
 // ---------------------------------------------------------------------------
 
+// Batched transform time per word at each scale, relative (GB300: 10^9
+// transform words per second of whole batched products at that scale, tiles
+// merged, last pass fused; scales below 9 and above 20 estimated).
+double batch_word_rate(int s) {
+  static const double rate[] = {1.0, 1.0, 1.0, 1.0, 1.2, 1.4, 1.7, 2.0, 2.3, 2.57, 4.77, 6.94,
+                                7.51, 6.9, 6.9, 6.66, 6.39, 6.08, 5.63, 5.66, 5.65};
+  return s < (int)(sizeof rate / sizeof rate[0]) ? rate[s] : 5.0;
+}
+
+// An unbalanced product nx x ny (nx >= ny) may run as P pieces of k limbs of
+// the longer operand, each through a transform of scale s2 < s sharing the
+// shorter operand's: 2P + 1 transforms of 2^s2 words against 3 of 2^s.  The
+// piece length is the most that keeps each piece's product within its
+// transform (k + ny - 1 <= 2^s2), rounded down to a multiple of 8 (the CRT
+// scan's vector loads stay within a piece), and at least ny, so that at most
+// two pieces overlap at any product position.  Returns the scale; sets k, P
+// (k = nx, P = 1: not split).
+int batch_split(u64 nx, u64 ny, int s, u64* k, u64* P) {
+  double best = 3.0 * (double)(1ull << s) / batch_word_rate(s);
+  int s_best = s;
+  *k = nx;
+  *P = 1;
+  for (int s2 = s - 1; s2 >= 2; --s2) {
+    const u64 L2 = 1ull << s2;
+    if (L2 + 1 < 2 * ny) break;
+    const u64 kk = (L2 - ny + 1) & ~7ull;
+    if (kk < ny || kk >= nx) continue;
+    const u64 pieces = (nx + kk - 1) / kk;
+    const double cost = (2.0 * pieces + 1.0) * (double)L2 / batch_word_rate(s2);
+    if (cost < 0.95 * best) {
+      best = cost;
+      s_best = s2;
+      *k = kk;
+      *P = pieces;
+    }
+  }
+  return s_best;
+}
+
 nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, const int* square, u64 count) {
   B->count = count;
   B->na.assign(na, na + count);
@@ -356,6 +397,7 @@ nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, c
   B->jobs.resize(count);
   B->off_a.assign(count, 0);
   B->off_b.assign(count, 0);
+  B->swap.assign(count, 0);
   std::vector<int> steps(count, 0);
   std::vector<int> fused_at(count, -1);  // step of the fused items, -1 without
   int max_s = 2;
@@ -369,6 +411,8 @@ nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, c
     J = nn::BatchJob{};
     J.na = na[j];
     J.nb = nb[j];
+    J.piece = na[j];
+    J.pieces = 1;
     J.ctr_base = B->n_ctrs;
     J.flag_base = B->n_flags;
     B->n_flags += (nn::u32)nn::scan_tiles(na[j] + nb[j]);
@@ -376,13 +420,19 @@ nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, c
       J.s = 0;
       steps[j] = 1;
     } else {
-      const int s = ntt_scale(na[j], nb[j]);
-      J.s = s;
       J.square = square ? square[j] : 0;
       if (J.square && na[j] != nb[j]) {
         c->err = "batch: a square needs equal operand sizes";
         return NN_ERR_INVALID;
       }
+      // operand 0 is the longer one; it may be split into pieces
+      B->swap[j] = na[j] < nb[j];
+      J.na = std::max(na[j], nb[j]);
+      J.nb = std::min(na[j], nb[j]);
+      J.piece = J.na;
+      int s = ntt_scale(J.na, J.nb);
+      if (c->batch_split && !J.square) s = batch_split(J.na, J.nb, s, &J.piece, &J.pieces);
+      J.s = s;
       max_s = std::max(max_s, s);
       const std::vector<nn::Pass> plan = c->passes(s);
       if (plan.size() > 4) {
@@ -415,7 +465,7 @@ nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, c
       }
       const int m = J.n_pass;
       if (c->batch_fused && m >= 2 && J.C[m - 1] == 2) {
-        // forward passes 0..m-2 of both operands, the first operand's last
+        // forward passes 0..m-2 of both operands, the second operand's last
         // pass (not for a square), the fused step, inverse passes m-2..0, CRT
         fused_at[j] = J.square ? m - 1 : m;
         steps[j] = fused_at[j] + m + 1;
@@ -423,7 +473,7 @@ nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, c
         steps[j] = 2 * m + 2;
       }
       B->off_a[j] = B->arena_words;
-      B->arena_words += 3ull << s;
+      B->arena_words += J.pieces * (3ull << s);
       if (!J.square) {
         B->off_b[j] = B->arena_words;
         B->arena_words += 3ull << s;
@@ -457,44 +507,40 @@ nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, c
       }
       const int m = J.n_pass;
       const u64 L = 1ull << J.s;
+      // items of pass k over operand 0's pieces (tiles numbered across them) or operand 1
       auto pass_items = [&](unsigned char kind, int k, int operand) {
-        const u64 tw = (u64)J.C[k] << J.R[k], tiles = L / tw;
+        const u64 tw = (u64)J.C[k] << J.R[k], tiles = (L / tw) * (operand == 0 ? J.pieces : 1);
         const u64 per = std::max<u64>(1, c->batch_item_words / tw);
         for (int pr = 0; pr < 3; ++pr)
           for (u64 t = 0; t < tiles; t += per) push(kind, k, pr, operand, t, std::min(per, tiles - t));
+      };
+      auto crt_items = [&] {
+        for (u64 t = 0; t < nn::scan_tiles(J.na + J.nb); ++t) push(nn::kItemCrt, 0, 0, 0, t);
       };
       if (const int f = fused_at[j]; f >= 0) {
         if (st < m - 1) {
           for (int op = 0; op < (J.square ? 1 : 2); ++op) pass_items(nn::kItemFwd, st, op);
         } else if (st < f) {
-          pass_items(nn::kItemFwd, m - 1, 0);  // the first operand's last pass
+          pass_items(nn::kItemFwd, m - 1, 1);  // the second operand's last pass
         } else if (st == f) {
           pass_items(nn::kItemFused, m - 1, 0);
         } else if (st < f + m) {
           pass_items(nn::kItemInv, f + m - 1 - st, 0);  // inverse passes m-2 .. 0
         } else {
-          for (u64 t = 0; t < nn::scan_tiles(J.na + J.nb); ++t) push(nn::kItemCrt, 0, 0, 0, t);
+          crt_items();
         }
         continue;
       }
       if (st < m) {  // forward pass st of each operand
-        const u64 tw = (u64)J.C[st] << J.R[st], tiles = L / tw;
-        const u64 per = std::max<u64>(1, c->batch_item_words / tw);
-        for (int op = 0; op < (J.square ? 1 : 2); ++op)
-          for (int pr = 0; pr < 3; ++pr)
-            for (u64 t = 0; t < tiles; t += per) push(nn::kItemFwd, st, pr, op, t, std::min(per, tiles - t));
+        for (int op = 0; op < (J.square ? 1 : 2); ++op) pass_items(nn::kItemFwd, st, op);
       } else if (st == m) {
-        const u64 chunks = (L / 4 + nn::kBatchPointwiseChunk - 1) / nn::kBatchPointwiseChunk;
+        const u64 chunks = (L / 4 + nn::kBatchPointwiseChunk - 1) / nn::kBatchPointwiseChunk * J.pieces;
         for (int pr = 0; pr < 3; ++pr)
           for (u64 t = 0; t < chunks; ++t) push(nn::kItemPointwise, 0, pr, 0, t);
       } else if (st < 2 * m + 1) {  // inverse passes m-1 .. 0
-        const int k = 2 * m - st;
-        const u64 tw = (u64)J.C[k] << J.R[k], tiles = L / tw;
-        const u64 per = std::max<u64>(1, c->batch_item_words / tw);
-        for (int pr = 0; pr < 3; ++pr)
-          for (u64 t = 0; t < tiles; t += per) push(nn::kItemInv, k, pr, 0, t, std::min(per, tiles - t));
+        pass_items(nn::kItemInv, 2 * m - st, 0);
       } else {
-        for (u64 t = 0; t < nn::scan_tiles(J.na + J.nb); ++t) push(nn::kItemCrt, 0, 0, 0, t);
+        crt_items();
       }
     }
   }
@@ -947,6 +993,8 @@ nn_status nn_context_set_tunable(nn_context* c, const char* name, int64_t v) {
     c->batch_fused = (int)v;
   else if (k == "batch_merge" && (v == 0 || v == 1))
     c->batch_merge = (int)v;
+  else if (k == "batch_split" && (v == 0 || v == 1))
+    c->batch_split = (int)v;
   else if (k == "batch_blocks_per_sm" && v >= 0 && v <= 32)
     c->batch_blocks_per_sm = (int)v;
   else {
@@ -973,6 +1021,7 @@ int64_t nn_context_get_tunable(const nn_context* c, const char* name) {
   if (k == "batch_item_words") return (int64_t)c->batch_item_words;
   if (k == "batch_fused") return (int64_t)c->batch_fused;
   if (k == "batch_merge") return (int64_t)c->batch_merge;
+  if (k == "batch_split") return (int64_t)c->batch_split;
   if (k == "batch_blocks_per_sm") return c->batch_blocks_per_sm;
   return -1;
 }
@@ -1000,8 +1049,8 @@ nn_status batch_fill(nn_context* c, nn_batch* B, const nn_mul_job* jobs, nn::Bat
       return NN_ERR_INVALID;
     }
     nn::BatchJob J = B->jobs[j];
-    J.a = jobs[j].d_a;
-    J.b = jobs[j].d_b;
+    J.a = B->swap[j] ? jobs[j].d_b : jobs[j].d_a;
+    J.b = B->swap[j] ? jobs[j].d_a : jobs[j].d_b;
     J.out = jobs[j].d_out;
     J.res_a = B->d_arena + B->off_a[j];
     J.res_b = B->d_arena + B->off_b[j];

@@ -66,12 +66,14 @@ constexpr u64 kBatchItemWords = 8192;
 constexpr u64 kBatchPointwiseChunk = 4096;
 enum : unsigned char { kItemFwd = 0, kItemPointwise = 1, kItemInv = 2, kItemCrt = 3, kItemColumn = 4, kItemFused = 5 };
 struct BatchJob {
-  const u64* a;
+  const u64* a;  // NTT jobs: the longer operand (split into pieces)
   const u64* b;
   u64* out;      // na + nb limbs
   u64 na, nb;
-  u64* res_a;    // [3][2^s] residues (NTT jobs)
-  u64* res_b;
+  u64* res_a;    // [pieces][3][2^s] residues (NTT jobs)
+  u64* res_b;    // [3][2^s]
+  u64 piece;     // limbs of a per piece (na when not split)
+  u64 pieces;
   u32 ctr_base;  // first (job, step) completion counter
   u32 flag_base; // first carry-scan status word
   int s;         // transform scale; 0 for a schoolbook job

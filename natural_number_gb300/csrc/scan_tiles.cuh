@@ -91,6 +91,61 @@ struct CrtProducerT {
 
 typedef CrtProducerT<false> CrtProducer;
 
+__device__ __forceinline__ W3 add_w3(W3 a, W3 b) {
+  W3 r;
+  r.w0 = a.w0 + b.w0;
+  const u64 c0 = r.w0 < a.w0;
+  const u64 t = a.w1 + b.w1;
+  const u64 c1 = t < a.w1;
+  r.w1 = t + c0;
+  r.w2 = a.w2 + b.w2 + c1 + (r.w1 < t);
+  return r;
+}
+
+// A product split into pieces: the longer operand x (nx limbs) cut into P
+// pieces of k limbs (the last one shorter), each multiplied by the shorter
+// operand y (ny <= k + 1 limbs) through its own transform of L words, laid
+// out [P][3][L].  Product coefficient j is the sum of coefficient j - i*k of
+// piece i = floor(j/k) (the last piece for j beyond it) and coefficient
+// j - (i-1)*k of piece i-1 when that is below k + ny - 1: at most two terms
+// (k >= ny - 1), each below 2^160, so the sum fits three limbs.  k is a
+// multiple of 8, so eight positions starting at a multiple of 8 lie in one
+// piece.  Batch work items read other CTAs' results: .cg loads.
+struct PieceCrtProducer {
+  const u64* res;
+  u64 L, k, P, ny, count;
+  static constexpr bool kBulk = true;
+  __device__ __forceinline__ CrtProducerT<true> piece(u64 i) const { return {res + i * 3 * L, L, L}; }
+  __device__ __forceinline__ u64 piece_of(u64 j) const {
+    const u64 i = j / k;
+    return i < P ? i : P - 1;
+  }
+  __device__ __forceinline__ W3 operator()(u64 j) const {
+    if (j >= count) return W3{0, 0, 0};
+    const u64 i = piece_of(j), r = j - i * k;
+    W3 x = piece(i)(r);
+    if (i > 0 && r + 1 < ny) x = add_w3(x, piece(i - 1)(r + k));
+    return x;
+  }
+  __device__ __forceinline__ void bulk(u64 k0, W3 (&x)[kScanE]) const {
+    if (k0 + kScanE > count) {
+#pragma unroll
+      for (int e = 0; e < kScanE; ++e) x[e] = (*this)(k0 + e);
+      return;
+    }
+    // one piece lookup for the eight positions; scalar loads keep fewer
+    // values live than two eight-position vector loads
+    const u64 i = piece_of(k0), r = k0 - i * k;
+    const CrtProducerT<true> cur = piece(i), prev = piece(i > 0 ? i - 1 : 0);
+    const bool ov = i > 0;
+#pragma unroll
+    for (int e = 0; e < kScanE; ++e) {
+      x[e] = cur(r + e);
+      if (ov && r + e + 1 < ny) x[e] = add_w3(x[e], prev(r + e + k));
+    }
+  }
+};
+
 // Column sums of a schoolbook product (asmMul1's column order, asmLinux.asm:188-278).
 struct ColumnProducer {
   static constexpr bool kBulk = false;
@@ -191,13 +246,30 @@ __device__ __forceinline__ u32 wait_flag(const u32* f, int limit) {
 // One tile of the scan over positions [0, total): limbs below out_limit go to
 // out, the rest to side.  Tiles of one scan must start in increasing order
 // (their predecessors already running), which the callers guarantee.
+// The scan's shared scratch: one block per kernel, whatever producers its
+// scan_tile instances take (a function's __shared__ variables exist once per
+// CTA, while each instance of a template would get its own).
+struct ScanShared {
+  u64 h0[kScanThreads], h1[kScanThreads];
+  u32 wg[kScanThreads / 32], wp[kScanThreads / 32];
+  u32 cin;
+  u64 x[kScanE][3];
+};
+__device__ __forceinline__ ScanShared& scan_shared() {
+  __shared__ ScanShared sh;
+  return sh;
+}
+
 template <class Prod>
 __device__ __forceinline__ void scan_tile(const Prod& prod, u64 tile, u64 total, u64* out, u64 out_limit, u64* side,
                                           u32* flags, u32* err) {
   constexpr int E = kScanE;
-  __shared__ u64 s_h0[kScanThreads], s_h1[kScanThreads];
-  __shared__ u32 s_wg[kScanThreads / 32], s_wp[kScanThreads / 32];
-  __shared__ u32 s_cin;
+  ScanShared& sh = scan_shared();
+  u64* const s_h0 = sh.h0;
+  u64* const s_h1 = sh.h1;
+  u32* const s_wg = sh.wg;
+  u32* const s_wp = sh.wp;
+  u32& s_cin = sh.cin;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const u64 k0 = tile * kScanTile + (u64)tid * E;
 
@@ -227,7 +299,7 @@ __device__ __forceinline__ void scan_tile(const Prod& prod, u64 tile, u64 total,
   s_h1[tid] = c1;
   // Overflow of the E positions before this tile: lanes 0..E-1 of warp 0
   // produce one value each, thread 0 chains them.
-  __shared__ u64 s_x[E][3];
+  u64(&s_x)[E][3] = sh.x;
   if (warp == 0) {
     if (lane < E && tile != 0) {
       const W3 x = prod(tile * kScanTile - E + lane);

@@ -128,3 +128,30 @@ def test_batch_merged_tiles_match_unmerged(ctx, oracle):
         assert np.array_equal(normalize(plain[k]), want), k
         assert np.array_equal(merged[k], plain[k]), k
         assert np.array_equal(merged2[k], plain[k]), k
+
+
+def test_batch_split_unbalanced_products(ctx, oracle):
+    """Unbalanced products split into pieces of the longer operand sharing
+    the shorter operand's transform (either operand the longer one), mixed
+    with balanced products, squares and schoolbook jobs: the same products as
+    unsplit, and the oracle's."""
+    sizes = [(262144, 200), (200, 262144), (100000, 3000), (3000, 100000), (65536, 8000), (5000, 128),
+             (300000, 129), (20000, 20000), (4096, 4096), (1000, 50), (150000, 20000), (2048, 2048)]
+    square = [0] * 10 + [0, 1]
+    a_list = [limbs(k + 701, x) for k, (x, _) in enumerate(sizes)]
+    b_list = [a_list[k] if square[k] else limbs(k + 801, y) for k, (_, y) in enumerate(sizes)]
+    old = ctx.get_tunable("batch_split")
+    try:
+        ctx.set_tunable("batch_split", 0)
+        whole, p0 = run_batch(ctx, a_list, b_list, square=square)
+        ctx.set_tunable("batch_split", 1)
+        split, p1 = run_batch(ctx, a_list, b_list, square=square)
+        split2, _ = run_batch(ctx, a_list, b_list, square=square, plan=p1)  # graph replay
+    finally:
+        ctx.set_tunable("batch_split", old)
+    assert p1.items != p0.items
+    for k in range(len(sizes)):
+        want = oracle.sqr(a_list[k]) if square[k] else oracle.mul(a_list[k], b_list[k])
+        assert np.array_equal(normalize(whole[k]), want), k
+        assert np.array_equal(split[k], whole[k]), k
+        assert np.array_equal(split2[k], whole[k]), k
