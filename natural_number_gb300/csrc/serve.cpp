@@ -72,7 +72,6 @@ struct nn_server {
   uint64_t peak = 0;
   nn_context* ctx = nullptr;
   std::vector<cudaStream_t> streams;
-  int next_stream = 0;
   std::vector<nn_context*> div_ctx;
   std::vector<cudaStream_t> div_streams;  // the division contexts' low-priority streams
   std::mutex mu;
@@ -80,6 +79,7 @@ struct nn_server {
   std::deque<Request*> waiting;
   std::deque<Request*> div_queue;
   std::vector<InFlight> inflight;
+  std::vector<Request*> ready;  // admitted products waiting for a free stream (scheduler thread)
   std::map<uint64_t, Request*> all;
   uint64_t next_id = 1;
   bool stop = false;
@@ -100,11 +100,17 @@ void finish(nn_server* S, Request* R, nn_status st) {
   S->in_use -= R->bytes;
 }
 
-// Launches every admitted, unlaunched multiply as one batch.
+// Launches every admitted, unlaunched multiply as one batch, on a stream
+// with no batch in flight.
 void launch_products(nn_server* S, std::vector<Request*>& fresh) {
   if (fresh.empty()) return;
-  const int k = S->next_stream;
-  S->next_stream = (S->next_stream + 1) % (int)S->streams.size();
+  int k = 0;
+  for (; k < (int)S->streams.size(); ++k) {
+    bool busy = false;
+    for (const InFlight& f : S->inflight) busy |= f.stream == k;
+    if (!busy) break;
+  }
+  if (k == (int)S->streams.size()) k = 0;  // not reached: the caller checks for a free stream
   cudaStream_t st = S->streams[k];
   nn_context_set_stream(S->ctx, st);
   std::vector<nn_mul_job> jobs;
@@ -184,10 +190,13 @@ bool retire(nn_server* S) {
   return any;
 }
 
+// Continuous batching: products admitted while every stream has a batch in
+// flight wait, and go out together in the next batch when one retires; so
+// under load the batches grow rather than the number of small launches.
 void scheduler(nn_server* S) {
   cudaSetDevice(S->device);
   while (true) {
-    std::vector<Request*> fresh;
+    std::vector<Request*>& fresh = S->ready;
     bool quit = false;
     {
       std::lock_guard<std::mutex> lk(S->mu);
@@ -207,13 +216,20 @@ void scheduler(nn_server* S) {
           S->div_cv.notify_one();
         }
       }
-      quit = S->stop && S->waiting.empty() && S->inflight.empty() && S->div_queue.empty() && S->div_running == 0;
+      quit = S->stop && S->waiting.empty() && S->inflight.empty() && S->div_queue.empty() && S->div_running == 0 &&
+             fresh.empty();
     }
     if (quit) break;
-    launch_products(S, fresh);  // no lock: only this thread touches the in-flight list and the context
+    // no lock: only this thread touches the ready and in-flight lists and the context
+    bool launched = false;
+    if (!fresh.empty() && S->inflight.size() < S->streams.size()) {
+      launch_products(S, fresh);
+      fresh.clear();
+      launched = true;
+    }
     const bool retired = retire(S);
     if (retired) S->done_cv.notify_all();
-    if (fresh.empty() && !retired) {
+    if (!launched && !retired) {
       std::unique_lock<std::mutex> lk(S->mu);
       S->cv.wait_for(lk, std::chrono::microseconds(S->inflight.empty() ? 2000 : 50));
     }
