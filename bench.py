@@ -333,6 +333,7 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the uneven-size batch measurement")
+    ap.add_argument("--batch-count", type=int, default=4096, help="products in the uneven-size batch")
     ap.add_argument("--no-serve", action="store_true", help="skip the served request stream")
     ap.add_argument("--serve-jobs", type=int, default=1000)
     ap.add_argument("--no-series", action="store_true", help="skip pi and e to 10^8 digits (a few seconds)")
@@ -420,7 +421,7 @@ def main() -> None:
 
     batched = None
     if not args.no_batch:
-        batched = measure_batched(ctx, args.steps, args.warmup)
+        batched = measure_batched(ctx, args.steps, args.warmup, args.batch_count)
     serving = None
     if not args.no_serve and rank == 0:
         from natural_number_gb300 import serving as serving_mod
