@@ -145,6 +145,8 @@ nn_status nn_batch_mul(nn_context* ctx, const nn_mul_job* jobs, uint64_t count);
 /* Tunables: "r_last" (levels of the contiguous NTT pass, 3..12, default 11),
  * "r_col" (most levels of a strided pass, 1..9, default 9), "r_last@<s>" and
  * "r_col@<s>" (the same for transforms of scale s only; 0 = default),
+ * "batch_r_last@<s>" (r_last for batched transforms of scale s; 0 = as for
+ * one product),
  * "batch_ntt_min" (default 384), "batch_blocks_per_sm" (0 = occupancy limit),
  * "batch_item_words" (residues per prime a batch pass item covers at least,
  * in consecutive tiles; default 8192), "batch_fused" (1, the default: a

@@ -49,10 +49,17 @@ struct nn_context {
   int r_col = 9;              // most levels of a strided column pass
   int r_last_at[64] = {};     // per-scale overrides (0: use r_last / r_col)
   int r_col_at[64] = {};
+  int batch_r_last_at[64] = {};  // per-scale overrides for batched transforms (0: as above)
   std::vector<nn::Pass> passes(int s) const {
     const int rl = (s >= 0 && s < 64 && r_last_at[s]) ? r_last_at[s] : r_last;
     const int rc = (s >= 0 && s < 64 && r_col_at[s]) ? r_col_at[s] : r_col;
     return nn::plan_passes(s, rl, rc);
+  }
+  // Batched transforms merge small tiles, which favours other splits at the
+  // scales where products are usually batched.
+  std::vector<nn::Pass> batch_passes(int s) const {
+    if (s < 0 || s >= 64 || !batch_r_last_at[s]) return passes(s);
+    return nn::plan_passes(s, batch_r_last_at[s], r_col_at[s] ? r_col_at[s] : r_col);
   }
   u64 batch_ntt_min = 384;    // batches: schoolbook when min(n_a, n_b) is below this
   u64 batch_item_words = nn::kBatchItemWords;  // residues a pass item covers at least
@@ -434,7 +441,7 @@ nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, c
       if (c->batch_split && !J.square) s = batch_split(J.na, J.nb, s, &J.piece, &J.pieces);
       J.s = s;
       max_s = std::max(max_s, s);
-      const std::vector<nn::Pass> plan = c->passes(s);
+      const std::vector<nn::Pass> plan = c->batch_passes(s);
       if (plan.size() > 4) {
         c->err = "batch: transform too long for one batch";
         return NN_ERR_INVALID;
@@ -970,12 +977,12 @@ nn_status nn_context_set_tunable(nn_context* c, const char* name, int64_t v) {
   if (!c || !name) return NN_ERR_INVALID;
   std::string k(name);
   const size_t at = k.find('@');
-  if (at != std::string::npos) {  // per-scale pass split: "r_last@28", "r_col@28"
+  if (at != std::string::npos) {  // per-scale pass split: "r_last@28", "r_col@28", "batch_r_last@16"
     const std::string base = k.substr(0, at);
     const int sc = std::atoi(k.c_str() + at + 1);
-    if (sc >= 2 && sc < 64 && ((base == "r_last" && (v == 0 || (v >= 3 && v <= 12))) ||
-                               (base == "r_col" && v >= 0 && v <= 9))) {
-      (base == "r_last" ? c->r_last_at : c->r_col_at)[sc] = (int)v;
+    const bool rl = base == "r_last" || base == "batch_r_last";
+    if (sc >= 2 && sc < 64 && ((rl && (v == 0 || (v >= 3 && v <= 12))) || (base == "r_col" && v >= 0 && v <= 9))) {
+      (base == "r_last" ? c->r_last_at : base == "r_col" ? c->r_col_at : c->batch_r_last_at)[sc] = (int)v;
       return NN_OK;
     }
     c->err = "unknown tunable or value out of range: " + k;
@@ -1013,6 +1020,7 @@ int64_t nn_context_get_tunable(const nn_context* c, const char* name) {
     if (sc < 2 || sc >= 64) return -1;
     if (k.substr(0, at) == "r_last") return c->r_last_at[sc];
     if (k.substr(0, at) == "r_col") return c->r_col_at[sc];
+    if (k.substr(0, at) == "batch_r_last") return c->batch_r_last_at[sc];
     return -1;
   }
   if (k == "r_last") return c->r_last;

@@ -110,19 +110,19 @@ def test_batch_merged_tiles_match_unmerged(ctx, oracle):
     a_list = [limbs(k + 501, x) for k, (x, _) in enumerate(sizes)]
     b_list = [a_list[k] if square[k] else limbs(k + 601, y) for k, (_, y) in enumerate(sizes)]
     old = ctx.get_tunable("batch_merge")
-    old_rl = {s: ctx.get_tunable("r_last@%d" % s) for s in (13, 16)}
+    old_rl = {s: ctx.get_tunable("batch_r_last@%d" % s) for s in (13, 16)}
     try:
         ctx.set_tunable("batch_merge", 0)
         plain, _ = run_batch(ctx, a_list, b_list, square=square)
         ctx.set_tunable("batch_merge", 1)
         merged, _ = run_batch(ctx, a_list, b_list, square=square)
-        ctx.set_tunable("r_last@13", 6)  # a 6-level strided pass widened to 32 columns
-        ctx.set_tunable("r_last@16", 7)
+        ctx.set_tunable("batch_r_last@13", 6)  # a 6-level strided pass widened to 32 columns
+        ctx.set_tunable("batch_r_last@16", 7)
         merged2, _ = run_batch(ctx, a_list, b_list, square=square)
     finally:
         ctx.set_tunable("batch_merge", old)
         for s, v in old_rl.items():
-            ctx.set_tunable("r_last@%d" % s, v)
+            ctx.set_tunable("batch_r_last@%d" % s, v)
     for k in range(len(sizes)):
         want = oracle.sqr(a_list[k]) if square[k] else oracle.mul(a_list[k], b_list[k])
         assert np.array_equal(normalize(plain[k]), want), k
