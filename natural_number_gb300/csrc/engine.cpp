@@ -398,6 +398,10 @@ int batch_split(u64 nx, u64 ny, int s, u64* k, u64* P) {
 }
 
 nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, const int* square, u64 count) {
+  if (count >= 0xffffffffull) {  // BatchItem::job is 32-bit
+    c->err = "batch: too many products";
+    return NN_ERR_INVALID;
+  }
   B->count = count;
   B->na.assign(na, na + count);
   B->nb.assign(nb, nb + count);
@@ -517,7 +521,7 @@ nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, c
       // items of pass k over operand 0's pieces (tiles numbered across them) or operand 1
       auto pass_items = [&](unsigned char kind, int k, int operand) {
         const u64 tw = (u64)J.C[k] << J.R[k], tiles = (L / tw) * (operand == 0 ? J.pieces : 1);
-        const u64 per = std::max<u64>(1, c->batch_item_words / tw);
+        const u64 per = std::clamp<u64>(c->batch_item_words / tw, 1, 0xffff);  // BatchItem::ntile is 16-bit
         for (int pr = 0; pr < 3; ++pr)
           for (u64 t = 0; t < tiles; t += per) push(kind, k, pr, operand, t, std::min(per, tiles - t));
       };

@@ -16,6 +16,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <bit>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -43,8 +44,24 @@ struct Request {
   int state = 0;  // 0 waiting, 1 admitted, 2 done
   nn_status status = NN_OK;
   uint64_t out_n = 0, q_n = 0, r_n = 0;
-  uint64_t *d_a = nullptr, *d_b = nullptr, *d_out = nullptr;
+  uint64_t *d_in = nullptr, *d_out = nullptr;  // d_in: a, then b from an even offset
+  uint64_t* stage = nullptr;                  // page-locked: a|b on the way in, the product on the way out
+  uint64_t stage_bytes = 0;
 };
+
+// Offset of b in a product request's input buffers (16-byte aligned).
+uint64_t b_offset(const Request* R) { return (R->na + 1) & ~1ull; }
+
+// Page-locked staging for a request's transfers, from the recycled host pool
+// in power-of-two sizes (so that blocks are reused across request sizes).
+uint64_t stage_size(uint64_t bytes) { return std::bit_ceil(std::max<uint64_t>(bytes, 64 << 10)); }
+
+void release_buffers(Request* R, cudaStream_t st) {
+  if (R->d_in) cudaFreeAsync(R->d_in, st);
+  if (R->d_out) cudaFreeAsync(R->d_out, st);
+  if (R->stage) nn_host_free(R->stage, R->stage_bytes);
+  R->d_in = R->d_out = R->stage = nullptr;
+}
 
 struct InFlight {
   std::vector<Request*> reqs;
@@ -116,19 +133,29 @@ void launch_products(nn_server* S, std::vector<Request*>& fresh) {
   std::vector<nn_mul_job> jobs;
   std::vector<Request*> ok;
   for (Request* R : fresh) {
-    cudaError_t e = cudaMallocAsync((void**)&R->d_a, R->na * 8, st);
-    if (e == cudaSuccess) e = cudaMallocAsync((void**)&R->d_b, R->nb * 8, st);
-    if (e == cudaSuccess) e = cudaMallocAsync((void**)&R->d_out, (R->na + R->nb) * 8, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(R->d_a, R->a, R->na * 8, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(R->d_b, R->b, R->nb * 8, cudaMemcpyHostToDevice, st);
+    // The client's (pageable) operands go through page-locked staging, filled
+    // on all host cores, so the link copies run at full speed and the
+    // scheduler thread is not held up by a driver-staged copy.
+    const uint64_t ob = b_offset(R), n_in = ob + R->nb, n_out = R->na + R->nb;
+    R->stage_bytes = stage_size(std::max(n_in, n_out) * 8);
+    R->stage = static_cast<uint64_t*>(nn_host_alloc(R->stage_bytes));
+    cudaError_t e = R->stage ? cudaSuccess : cudaErrorMemoryAllocation;
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&R->d_in, n_in * 8, st);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&R->d_out, n_out * 8, st);
+    if (e == cudaSuccess) {
+      nn_host_copy(R->stage, R->a, R->na);
+      nn_host_copy(R->stage + ob, R->b, R->nb);
+      e = cudaMemcpyAsync(R->d_in, R->stage, n_in * 8, cudaMemcpyHostToDevice, st);
+    }
     if (e != cudaSuccess) {
       cudaGetLastError();
+      release_buffers(R, st);
       std::lock_guard<std::mutex> lk(S->mu);
       finish(S, R, e == cudaErrorMemoryAllocation ? NN_ERR_OOM : NN_ERR_CUDA);
       S->done_cv.notify_all();
       continue;
     }
-    jobs.push_back(nn_mul_job{R->d_a, R->na, R->d_b, R->nb, R->d_out});
+    jobs.push_back(nn_mul_job{R->d_in, R->na, R->d_in + ob, R->nb, R->d_out});
     ok.push_back(R);
   }
   if (ok.empty()) return;
@@ -140,6 +167,12 @@ void launch_products(nn_server* S, std::vector<Request*>& fresh) {
   InFlight f;
   nn_status bs = nn_batch_create(S->ctx, na.data(), nb.data(), nullptr, ok.size(), &f.batch);
   if (bs == NN_OK) bs = nn_batch_launch(S->ctx, f.batch, jobs.data());
+  if (bs == NN_OK)  // the products come back into the staging behind the batch, on its stream
+    for (Request* R : ok)
+      if (cudaMemcpyAsync(R->stage, R->d_out, (R->na + R->nb) * 8, cudaMemcpyDeviceToHost, st) != cudaSuccess) {
+        cudaGetLastError();
+        R->status = NN_ERR_CUDA;
+      }
   f.reqs = ok;
   f.stream = k;
   cudaEventCreateWithFlags(&f.done, cudaEventDisableTiming);
@@ -165,18 +198,14 @@ bool retire(nn_server* S) {
     }
     cudaStream_t st = S->streams[f.stream];
     for (Request* R : f.reqs) {
-      // the batch is complete: copy the product into the client's (pageable) buffer now
-      if (R->status == NN_OK &&
-          cudaMemcpy(R->out, R->d_out, (R->na + R->nb) * 8, cudaMemcpyDeviceToHost) != cudaSuccess) {
-        cudaGetLastError();
-        R->status = NN_ERR_CUDA;
-      }
+      // the batch and its copies are complete: the product is in the staging
       uint64_t n = R->na + R->nb;
-      while (n > 1 && R->out[n - 1] == 0) --n;
+      if (R->status == NN_OK) {
+        nn_host_copy(R->out, R->stage, n);
+        while (n > 1 && R->out[n - 1] == 0) --n;
+      }
       R->out_n = n;
-      cudaFreeAsync(R->d_a, st);
-      cudaFreeAsync(R->d_b, st);
-      cudaFreeAsync(R->d_out, st);
+      release_buffers(R, st);
     }
     {
       std::lock_guard<std::mutex> lk(S->mu);
