@@ -155,3 +155,21 @@ def test_batch_split_unbalanced_products(ctx, oracle):
         assert np.array_equal(normalize(whole[k]), want), k
         assert np.array_equal(split[k], whole[k]), k
         assert np.array_equal(split2[k], whole[k]), k
+
+
+def test_batch_tiny_transforms_with_largest_items(ctx, oracle):
+    """Every product on the NTT route, down to transforms of 4 words, with the
+    largest item size: an item's tile count is capped at its 16-bit field."""
+    sizes = [(1, 1), (2, 3), (5, 5), (9, 7), (33, 31), (130, 2), (1000, 1000)]
+    a_list = [limbs(k + 901, x) for k, (x, _) in enumerate(sizes)]
+    b_list = [limbs(k + 951, y) for k, (_, y) in enumerate(sizes)]
+    old = {k: ctx.get_tunable(k) for k in ("batch_ntt_min", "batch_item_words")}
+    try:
+        ctx.set_tunable("batch_ntt_min", 1)
+        ctx.set_tunable("batch_item_words", 1 << 20)
+        outs, _ = run_batch(ctx, a_list, b_list)
+    finally:
+        for k, v in old.items():
+            ctx.set_tunable(k, v)
+    for k in range(len(sizes)):
+        assert np.array_equal(normalize(outs[k]), oracle.mul(a_list[k], b_list[k])), k
