@@ -95,8 +95,8 @@ nn_status nn_sqr(nn_context* ctx, uint64_t* d_out, const uint64_t* d_a, uint64_t
 nn_status nn_ntt_mul(nn_context* ctx, uint64_t* d_out, const uint64_t* d_a, uint64_t n_a, const uint64_t* d_b,
                      uint64_t n_b, int scale, uint64_t size, uint64_t* written);
 /* Quotient and remainder with every step on the GPU: an exact Newton division
- * of this build's own (normalisation, a Newton reciprocal with precision
- * doubling, one quotient estimate and at most a few corrections).  Quotient
+ * (normalisation, a Newton reciprocal with precision doubling, one quotient
+ * estimate and at most a few corrections), not the reference's algorithm.  Quotient
  * and remainder are unique, so they equal natural::_div's (natural.h:749-769).
  * q gets n_a - n_b + 1 limbs and r n_b limbs, not normalised; n_a >= n_b >= 1
  * and the divisor's top limb is nonzero.  nn_div takes device pointers and

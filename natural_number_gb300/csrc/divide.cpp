@@ -3,8 +3,8 @@
 // The reference divides (natural::_div, div_iterative and the Newton
 // reciprocal, natural.h:620-769) on the host around its products; the
 // drop-in header keeps that algorithm step for step.  Quotient and remainder
-// are unique, so for long operands the C entry points here use a division of
-// this build's own whose every step stays in HBM, and the results are the
+// are unique, so for long operands the C entry points here use a different
+// division whose every step stays in HBM, and the results are the
 // reference's:
 //   1. normalise: D = b << cl (top bit set), A = a << cl (na + 1 limbs);
 //   2. V ~ floor(B^(2t) / D_t) by Newton's method with precision doubling,
