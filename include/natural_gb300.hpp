@@ -882,7 +882,12 @@ inline natural operator%(const natural& a, const natural& b) {
   return r;
 }
 
-// natural.h:795-839
+// natural.h:795-839.  n! = 2^e2 * prod over odd primes p of p^e_p, built by
+// Horner's rule over the bits of the exponents: at bit i, ans = ans^2 times
+// the product of the primes whose exponent has bit i set (a balanced product
+// through a min-queue).  Where no odd prime's exponent has bit i set (n = 9:
+// 3^4 5 7) the reference reads the top of an empty queue; here that factor is
+// 1, the value the formula means.
 inline natural factorial(uint64_t n) {
   if (n <= 1) return 1;
   if (n == 2) return 2;
@@ -914,7 +919,8 @@ inline natural factorial(uint64_t n) {
       pq.pop();
       pq.push(n1 * n2);
     }
-    ans = sqr(ans) * pq.top();
+    ans = sqr(ans);
+    if (!pq.empty()) ans *= pq.top();
   }
   ans <<= prime_exp[0];
   return ans;
@@ -1052,6 +1058,10 @@ inline natural& natural::hex(std::string_view sv) {  // natural.h:121-143
 }
 inline natural& natural::dec(std::string_view sv) {  // natural.h:925-941
   using namespace nn_gb300;
+  if (sv.empty()) {  // the reference's index arithmetic below underflows (i = 63) on ""
+    *this = 0;
+    return *this;
+  }
   int i = 63 - std::countl_zero((uint64_t)((sv.size() + dec_length - 1) / dec_length - 1));
   if (i == -1) {
     *this = 0;

@@ -99,6 +99,11 @@ def test_cpp_dropin_program(golden, tmp_path):
     import math
     assert int(out[4]) == math.factorial(2000)
     assert out[5] == "dec ok" and out[6] == "hex ok"
+    ns = list(range(41)) + [63, 64, 100, 127, 128, 255, 1000]
+    assert [int(v) for v in out[7].split()] == [math.factorial(n) for n in ns]
+    strs = ["0", "7", "18446744073709551615", "18446744073709551616", "000123", "",
+            "340282366920938463463374607431768211456"]
+    assert [int(v, 16) for v in out[8].split()] == [int(t) if t else 0 for t in strs]
 
 
 # Divisions on which the reference's own Newton division aborts
