@@ -242,11 +242,15 @@ nn_status nn_sqr_host(nn_context* ctx, uint64_t* out, uint64_t* out_n, const uin
 void nn_free(void* p);
 /* Page-locked host memory for limb buffers (the drop-in natural's buffers of
  * 64 KiB and more): copies between such buffers and the GPU run at the host
- * link's speed.  Blocks are recycled by size; nn_host_alloc falls back to
- * malloc when no page-locked memory can be had, and nn_host_free takes either
- * kind (bytes = the size passed to nn_host_alloc).  Thread-safe. */
+ * link's speed.  Blocks are powers of two (at least 64 KiB) from a buddy
+ * allocator over page-locked slabs of 64 MiB to 1 GiB, so freed blocks merge
+ * and serve later requests of any size; larger requests get their own block.
+ * Without page-locked memory the slabs are ordinary memory.  nn_host_free
+ * takes bytes = the size passed to nn_host_alloc.  Thread-safe. */
 void* nn_host_alloc(uint64_t bytes);
 void nn_host_free(void* p, uint64_t bytes);
+/* Host bytes the pool holds (its slabs, and free blocks above 1 GiB). */
+uint64_t nn_host_pool_reserved(void);
 /* Host limb arithmetic for long operands, run on all host cores with the
  * results of the sequential loops (asmAdd0/asmSub0/asmShl/asmShr, asm.h:7-33):
  * the drop-in natural's O(n) steps between GPU products.  add/sub return the

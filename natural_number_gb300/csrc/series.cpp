@@ -233,12 +233,13 @@ struct Pinned {
   u64* p = nullptr;
   u64 cap = 0;
   u64* get(u64 words) {
-    if (words > cap) {
-      if (p) cudaFreeHost(p);
+    if (words > cap) {  // from the recycled page-locked pool, so later calls pin nothing new
+      if (p) nn_host_free(p, 8 * cap);
       p = nullptr;
       cap = 0;
       const u64 w = std::max<u64>(words + words / 4, 1 << 16);
-      check_cuda(cudaHostAlloc((void**)&p, 8 * w, cudaHostAllocDefault), "pinned staging");
+      p = static_cast<u64*>(nn_host_alloc(8 * w));
+      if (!p) throw std::bad_alloc();
       cap = w;
     }
     return p;
@@ -247,7 +248,7 @@ struct Pinned {
   Pinned(const Pinned&) = delete;
   Pinned& operator=(const Pinned&) = delete;
   ~Pinned() {
-    if (p) cudaFreeHost(p);
+    if (p) nn_host_free(p, 8 * cap);
   }
 };
 
