@@ -25,6 +25,7 @@
 #include <cstdio>
 #include <cstring>
 #include <exception>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -268,44 +269,89 @@ struct Products {
   u64 size() const { return out.size(); }
 };
 
+// Operands and products at least this long cross the host link straight
+// from and into their own buffers (the drop-in natural keeps those
+// page-locked); shorter ones are packed into the staging, one copy each way.
+constexpr u64 kDirectLimbs = 1 << 14;
+
 void run_products(nn_context* c, Products& P, Staging& stg, Stats& S) {
   const u64 m = P.size();
   if (!m) return;
   const auto t0 = Clock::now();
   std::vector<u64> na(m), nb(m), oa(m), ob(m), oo(m);
+  // device layout: the short operands (and products) packed first, so that
+  // one copy moves them; the long ones after
   u64 tin = 0, tout = 0;
+  for (int pass = 0; pass < 2; ++pass)
+    for (u64 k = 0; k < m; ++k) {
+      na[k] = P.a[k]->size;
+      nb[k] = P.b[k]->size;
+      // even offsets: the kernels read 16-byte aligned operands with vector loads
+      if ((na[k] >= kDirectLimbs) == (pass == 1)) {
+        oa[k] = tin;
+        tin = (tin + na[k] + 1) & ~1ull;
+      }
+      if ((nb[k] >= kDirectLimbs) == (pass == 1)) {
+        ob[k] = tin;
+        tin = (tin + nb[k] + 1) & ~1ull;
+      }
+      if ((na[k] + nb[k] >= kDirectLimbs) == (pass == 1)) {
+        oo[k] = tout;
+        tout = (tout + na[k] + nb[k] + 1) & ~1ull;
+      }
+    }
+  u64 tin_small = 0, tout_small = 0;
   for (u64 k = 0; k < m; ++k) {
-    na[k] = P.a[k]->size;
-    nb[k] = P.b[k]->size;
-    oa[k] = tin;
-    tin += na[k];
-    ob[k] = tin;
-    tin += nb[k];
-    oo[k] = tout;
-    tout += na[k] + nb[k];
+    if (na[k] < kDirectLimbs) tin_small = std::max(tin_small, oa[k] + na[k]);
+    if (nb[k] < kDirectLimbs) tin_small = std::max(tin_small, ob[k] + nb[k]);
+    if (na[k] + nb[k] < kDirectLimbs) tout_small = std::max(tout_small, oo[k] + na[k] + nb[k]);
   }
-  u64* hin = stg.in.get(tin);
-  u64* hout = stg.out.get(tout);
+  u64* hin = stg.in.get(std::max<u64>(tin_small, 1));
+  u64* hout = stg.out.get(std::max<u64>(tout_small, 1));
   parallel_for(m, 256, [&](u64 k) {
-    std::memcpy(hin + oa[k], P.a[k]->data, 8 * na[k]);
-    std::memcpy(hin + ob[k], P.b[k]->data, 8 * nb[k]);
+    if (na[k] < kDirectLimbs) std::memcpy(hin + oa[k], P.a[k]->data, 8 * na[k]);
+    if (nb[k] < kDirectLimbs) std::memcpy(hin + ob[k], P.b[k]->data, 8 * nb[k]);
   });
   cudaStream_t st = (cudaStream_t)nn_context_stream(c);
   u64 *din = nullptr, *dout = nullptr;
   check_cuda(cudaMallocAsync((void**)&din, 8 * tin, st), "batch operands");
   check_cuda(cudaMallocAsync((void**)&dout, 8 * tout, st), "batch products");
-  check_cuda(cudaMemcpyAsync(din, hin, 8 * tin, cudaMemcpyHostToDevice, st), "upload");
+  if (tin_small) check_cuda(cudaMemcpyAsync(din, hin, 8 * tin_small, cudaMemcpyHostToDevice, st), "upload");
+  for (u64 k = 0; k < m; ++k) {
+    if (na[k] >= kDirectLimbs)
+      check_cuda(cudaMemcpyAsync(din + oa[k], P.a[k]->data, 8 * na[k], cudaMemcpyHostToDevice, st), "upload");
+    if (nb[k] >= kDirectLimbs)
+      check_cuda(cudaMemcpyAsync(din + ob[k], P.b[k]->data, 8 * nb[k], cudaMemcpyHostToDevice, st), "upload");
+  }
   std::vector<nn_mul_job> jobs(m);
   for (u64 k = 0; k < m; ++k) jobs[k] = nn_mul_job{din + oa[k], na[k], din + ob[k], nb[k], dout + oo[k]};
+  // long products land in fresh naturals, moved into place after the copies
+  // (an output may be one of the operands)
+  std::vector<std::unique_ptr<natural>> big(m);
   nn_batch* B = nullptr;
   nn_status s = nn_batch_create(c, na.data(), nb.data(), nullptr, m, &B);
   if (s == NN_OK) s = nn_batch_launch(c, B, jobs.data());
-  if (s == NN_OK) check_cuda(cudaMemcpyAsync(hout, dout, 8 * tout, cudaMemcpyDeviceToHost, st), "download");
+  if (s == NN_OK) {
+    if (tout_small)
+      check_cuda(cudaMemcpyAsync(hout, dout, 8 * tout_small, cudaMemcpyDeviceToHost, st), "download");
+    for (u64 k = 0; k < m; ++k)
+      if (na[k] + nb[k] >= kDirectLimbs) {
+        big[k] = std::make_unique<natural>();
+        big[k]->resize(na[k] + nb[k]);
+        check_cuda(cudaMemcpyAsync(big[k]->data, dout + oo[k], 8 * (na[k] + nb[k]), cudaMemcpyDeviceToHost, st),
+                   "download");
+      }
+  }
   if (B) nn_batch_destroy(c, B);
   cudaFreeAsync(din, st);
   cudaFreeAsync(dout, st);
   nn_gb300::check(s == NN_OK ? nn_context_synchronize(c) : s, "batched products");
-  parallel_for(m, 64, [&](u64 k) { *P.out[k] = to_natural(hout + oo[k], norm(hout + oo[k], na[k] + nb[k])); });
+  parallel_for(m, 64, [&](u64 k) {
+    if (big[k])
+      *P.out[k] = std::move(big[k]->std());
+    else
+      *P.out[k] = to_natural(hout + oo[k], norm(hout + oo[k], na[k] + nb[k]));
+  });
   S.gpu_s += since(t0);
   S.gpu_products += m;
   S.batches += 1;
