@@ -81,6 +81,21 @@ def measured_traffic(kernel: str, L: int):
     return None
 
 
+def measured_instructions(kernel: str, L: int):
+    """Warp instructions per launch from the committed ncu summary
+    profiles/instructions.txt (`<kernel> <instructions per launch> <L of the
+    capture>`), scaled by L like measured_traffic."""
+    path = os.path.join(ROOT, "profiles", "instructions.txt")
+    try:
+        for line in open(path):
+            f = line.split()
+            if len(f) >= 3 and f[0] == kernel and not line.startswith("#"):
+                return float(f[1]) * L / float(f[2])
+    except OSError:
+        pass
+    return None
+
+
 def peaks() -> tuple[float, str]:
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -408,13 +423,20 @@ def main() -> None:
         for _ in range(2):
             ctx.mul(ha, hb, out=ho)
         replicas.barrier(dist)
+        step_ms = []
         t0 = time.perf_counter()
         for _ in range(args.steps):
+            t1 = time.perf_counter()
             ctx.mul(ha, hb, out=ho)
+            step_ms.append((time.perf_counter() - t1) * 1e3)
         e_ms = (time.perf_counter() - t0) / args.steps * 1e3
         e_ms = replicas.max_over_ranks(e_ms, dist, "cuda")
+        # value: the mean over the K steps; the spread shows host-side stalls
+        # (the host link and memory are shared with other jobs on the machine)
         e2e = {"value": replicas.aggregate_rate(2 * n, world, e_ms), "unit": UNIT, "ms_per_step": e_ms,
-               "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 16 * n}
+               "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 16 * n,
+               "step_ms_median": statistics.median(step_ms), "step_ms_min": min(step_ms),
+               "step_ms_max": max(step_ms)}
 
     square = measure_square(ctx, da, n, args.steps, args.warmup)
     division = measure_division(ctx, cpu=not args.no_cpu) if rank == 0 and not args.no_div else None
@@ -439,6 +461,18 @@ def main() -> None:
     achieved = d_bytes / (d_avg / 1e3) / 1e9
     traffic = measured_traffic(dname, L)
     mul_bytes = mul_algorithmic_bytes(n, n, L)
+    clocks = clk.summary()
+    # The kernels are bound by integer issue, not HBM: one warp instruction
+    # per scheduler (4 per SM) per cycle at the sampled SM clock is the peak.
+    inst = measured_instructions(dname, L)
+    issue = None
+    if inst and clocks.get("sm_mhz"):
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        ipeak = 4.0 * sms * clocks["sm_mhz"] * 1e6
+        iach = inst / (d_avg / 1e3)
+        issue = {"bound": "int_issue", "kernel": dname, "achieved": iach, "peak": ipeak, "unit": "warp inst/s",
+                 "frac": iach / ipeak, "inst_per_launch": inst,
+                 "source": "profiles/instructions.txt (ncu at L = 2^23, scaled by L); peak 4 per SM per cycle"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
@@ -456,8 +490,10 @@ def main() -> None:
                          "frac": mul_bytes / (ms / 1e3) / 1e9 / peak},
         "kernels": {k: {"launches_per_step": c / args.steps, "ms_per_step": t / args.steps} for k, (c, t) in prof.items()},
         "gpu_launches": launches,
-        "clocks": clk.summary(),
+        "clocks": clocks,
     }
+    if issue:
+        line["issue_roofline"] = issue
     line["square"] = square
     if division:
         line["division"] = division
