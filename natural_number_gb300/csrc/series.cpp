@@ -623,7 +623,8 @@ u64 dec_subtree(const std::vector<DecLevel>& D, const u64* v, u64 nv, int i, boo
 
 // Decimal digits (std::formatter<natural>, natural.h:1089-1091): the split
 // tree of _format_dec, level by level with GPU batches while the split
-// powers are at least host_below limbs, then whole subtrees on host threads.
+// powers are at least host_below / 2 limbs, then whole subtrees on host
+// threads.
 std::string to_dec_levels(nn_context* c, const natural& x, u64 host_below, Staging& stg, Stats& S) {
   using namespace nn_gb300;
   const int top = dec_init(x);
@@ -642,7 +643,11 @@ std::string to_dec_levels(nn_context* c, const natural& x, u64 host_below, Stagi
   std::vector<Node> lv;
   lv.push_back(Node{x, true});
   int i = top;
-  for (; i >= 1 && std::min(D[i].nb, D[i].nr) >= host_below; --i) {
+  // GPU levels down to half the tree's threshold: below it a host subtree's
+  // O(n^2) schoolbook splits cost more than another batched level (measured
+  // on GB300 for pi and e to 10^8 digits: 128 limbs at the default 256)
+  const u64 dec_below = std::max<u64>(host_below / 2, 16);
+  for (; i >= 1 && std::min(D[i].nb, D[i].nr) >= dec_below; --i) {
     const natural& base = C.base[i];
     const natural& base_r = C.base_r[i];
     const u64 n = lv.size();
