@@ -219,6 +219,28 @@ __device__ __forceinline__ void tile_forward(u64* sm, int R, u64 ksb, const u64*
   }
 }
 
+// The same with R and the first level known at compile time (256 threads):
+// the unrolled group schedule makes every group's stride, unit count and
+// twiddle offset a constant, so the index arithmetic folds away.
+__host__ __device__ constexpr int group_cap_ct(int C, int R) {
+  int k = R < kMaxGroupLevels ? R : kMaxGroupLevels;
+  while (k > 1 && (C << (R - k)) < 256) --k;
+  return k;
+}
+template <int C, int PR, int R, int L0>
+__device__ __forceinline__ void tile_forward_ct(u64* sm, u64 ksb, const u64* tw, const u64* tws) {
+  constexpr int cap = group_cap_ct(C, R);
+  constexpr int n = (R - L0 + cap - 1) / cap;
+  int l = L0;
+#pragma unroll
+  for (int g = 0; g < n; ++g) {
+    const int k = (R - l + (n - g) - 1) / (n - g);
+    run_group<C, false, PR>(sm, k, l, R, ksb, tw, tws);
+    __syncthreads();
+    l += k;
+  }
+}
+
 // Inverse levels R-1 .. l_stop of the tile in shared memory.
 template <int C, int PR>
 __device__ __forceinline__ void tile_inverse(u64* sm, int R, u64 ksb, const u64* tw, const u64* tws, int l_stop = 0) {
@@ -230,6 +252,52 @@ __device__ __forceinline__ void tile_inverse(u64* sm, int R, u64 ksb, const u64*
     run_group<C, true, PR>(sm, k, l, R, ksb, tw, tws);
     __syncthreads();
   }
+}
+template <int C, int PR, int R, int LSTOP>
+__device__ __forceinline__ void tile_inverse_ct(u64* sm, u64 ksb, const u64* tw, const u64* tws) {
+  constexpr int cap = group_cap_ct(C, R);
+  constexpr int n = (R - LSTOP + cap - 1) / cap;
+  int l = R;
+#pragma unroll
+  for (int g = 0; g < n; ++g) {
+    const int k = (l - LSTOP + (n - g) - 1) / (n - g);
+    l -= k;
+    run_group<C, true, PR>(sm, k, l, R, ksb, tw, tws);
+    __syncthreads();
+  }
+}
+
+// Forward levels [l0, R) / inverse levels R-1 .. l_stop: the compile-time
+// schedules for the tile shapes of the large transforms' pass plans (strided
+// passes of 7-9 levels, contiguous passes of 10-11), the runtime loop
+// otherwise.  Only the per-call kernels take them (CT); the batch kernel
+// keeps one code path per width.
+template <int C, int PR, bool CT>
+__device__ __forceinline__ void tile_forward_any(u64* sm, int R, u64 ksb, const u64* tw, const u64* tws, int l0) {
+  if constexpr (CT && C == 2) {
+    if (R == 11 && l0 == 0) return tile_forward_ct<C, PR, 11, 0>(sm, ksb, tw, tws);
+    if (R == 10 && l0 == 0) return tile_forward_ct<C, PR, 10, 0>(sm, ksb, tw, tws);
+  } else if constexpr (CT && C == 16) {
+    if (R == 8 && l0 == 0) return tile_forward_ct<C, PR, 8, 0>(sm, ksb, tw, tws);
+    if (R == 8 && l0 == 1) return tile_forward_ct<C, PR, 8, 1>(sm, ksb, tw, tws);
+    if (R == 9 && l0 == 0) return tile_forward_ct<C, PR, 9, 0>(sm, ksb, tw, tws);
+    if (R == 9 && l0 == 1) return tile_forward_ct<C, PR, 9, 1>(sm, ksb, tw, tws);
+    if (R == 7 && l0 == 0) return tile_forward_ct<C, PR, 7, 0>(sm, ksb, tw, tws);
+    if (R == 7 && l0 == 1) return tile_forward_ct<C, PR, 7, 1>(sm, ksb, tw, tws);
+  }
+  tile_forward<C, PR>(sm, R, ksb, tw, tws, l0);
+}
+template <int C, int PR, bool CT>
+__device__ __forceinline__ void tile_inverse_any(u64* sm, int R, u64 ksb, const u64* tw, const u64* tws, int l_stop) {
+  if constexpr (CT && C == 2) {
+    if (R == 11 && l_stop == 0) return tile_inverse_ct<C, PR, 11, 0>(sm, ksb, tw, tws);
+    if (R == 10 && l_stop == 0) return tile_inverse_ct<C, PR, 10, 0>(sm, ksb, tw, tws);
+  } else if constexpr (CT && C == 16) {
+    if (R == 8 && l_stop == 0) return tile_inverse_ct<C, PR, 8, 0>(sm, ksb, tw, tws);
+    if (R == 9 && l_stop == 0) return tile_inverse_ct<C, PR, 9, 0>(sm, ksb, tw, tws);
+    if (R == 7 && l_stop == 0) return tile_inverse_ct<C, PR, 7, 0>(sm, ksb, tw, tws);
+  }
+  tile_inverse<C, PR>(sm, R, ksb, tw, tws, l_stop);
 }
 
 // Pointwise product of one group of 4 residues (a0..a3)(b0..b3), lazy forward
@@ -315,7 +383,7 @@ __device__ __forceinline__ void pass_tile_p(u64* sm, const u64* in, u64* out, u6
   __syncthreads();
 
   if (!INV) {
-    tile_forward<C, PR>(sm, R, ksb, tw, tws, half ? 1 : skip);
+    tile_forward_any<C, PR, !CG>(sm, R, ksb, tw, tws, half ? 1 : skip);
     if (FUSED) {  // contiguous tile: smem index == position - base; other == nullptr squares
       const u64* oth = other ? other + (u64)PR * L : nullptr;
       const ulonglong2* twsv = reinterpret_cast<const ulonglong2*>(tws);
@@ -340,10 +408,10 @@ __device__ __forceinline__ void pass_tile_p(u64* sm, const u64* in, u64* out, u6
       stage_twiddles(tws, itw, ksb, R);
       cp_async_wait_all();
       __syncthreads();
-      tile_inverse<C, PR>(sm, R, ksb, itw, tws, skip);
+      tile_inverse_any<C, PR, !CG>(sm, R, ksb, itw, tws, skip);
     }
   } else {
-    tile_inverse<C, PR>(sm, R, ksb, tw, tws, skip);
+    tile_inverse_any<C, PR, !CG>(sm, R, ksb, tw, tws, skip);
   }
 
   u64* dst = out + (u64)PR * L;
