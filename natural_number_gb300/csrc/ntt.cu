@@ -118,8 +118,9 @@ __global__ void __launch_bounds__(256, BLOCKS) ntt_fused_kernel(u64* res, const 
                                                              const u64* __restrict__ tab,
                                                              const u64* __restrict__ itab, u64 tab_stride) {
   extern __shared__ u64 sm[];
-  pass_tile<2, false, false, false, false, true>(sm, res, res, 0, s, lambda0, R, tab, tab_stride, blockIdx.y,
-                                                 blockIdx.x, itab, other);
+  // three CTAs an SM leave 80 registers a thread: room for radix-16 groups
+  pass_tile<2, false, false, false, false, true, BLOCKS == 3 ? 4 : 3>(sm, res, res, 0, s, lambda0, R, tab, tab_stride,
+                                                                     blockIdx.y, blockIdx.x, itab, other);
 }
 
 __global__ void __launch_bounds__(256) pointwise_kernel(u64* dst, const u64* a, const u64* b, u64 L,

@@ -220,25 +220,29 @@ __device__ __forceinline__ void tile_forward(u64* sm, int R, u64 ksb, const u64*
 }
 
 // The same with R and the first level known at compile time (256 threads):
-// the unrolled group schedule makes every group's stride, unit count and
-// twiddle offset a constant, so the index arithmetic folds away.
-__host__ __device__ constexpr int group_cap_ct(int C, int R) {
-  int k = R < kMaxGroupLevels ? R : kMaxGroupLevels;
+// the group schedule unrolls by template recursion, so every group's size,
+// stride, unit count and twiddle offsets are constants and the index
+// arithmetic folds away.  MAXK = 4 (radix-16 units) where the kernel has the
+// registers for 16 residues per thread: the fused pass, at 11 levels (4 + 4
+// + 3, one unit per thread).
+__host__ __device__ constexpr int group_cap_ct(int C, int R, int maxk) {
+  int k = R < maxk ? R : maxk;
   while (k > 1 && (C << (R - k)) < 256) --k;
   return k;
 }
-template <int C, int PR, int R, int L0>
-__device__ __forceinline__ void tile_forward_ct(u64* sm, u64 ksb, const u64* tw, const u64* tws) {
-  constexpr int cap = group_cap_ct(C, R);
-  constexpr int n = (R - L0 + cap - 1) / cap;
-  int l = L0;
-#pragma unroll
-  for (int g = 0; g < n; ++g) {
-    const int k = (R - l + (n - g) - 1) / (n - g);
-    run_group<C, false, PR>(sm, k, l, R, ksb, tw, tws);
+template <int C, int PR, int R, int L, int N, int G>
+__device__ __forceinline__ void fwd_groups_ct(u64* sm, u64 ksb, const u64* tw, const u64* tws) {
+  if constexpr (G < N) {
+    constexpr int K = (R - L + (N - G) - 1) / (N - G);
+    level_group<K, C, false, PR>(sm, L, R, ksb, tw, tws);
     __syncthreads();
-    l += k;
+    fwd_groups_ct<C, PR, R, L + K, N, G + 1>(sm, ksb, tw, tws);
   }
+}
+template <int C, int PR, int R, int L0, int MAXK = 3>
+__device__ __forceinline__ void tile_forward_ct(u64* sm, u64 ksb, const u64* tw, const u64* tws) {
+  constexpr int cap = group_cap_ct(C, R, MAXK);
+  fwd_groups_ct<C, PR, R, L0, (R - L0 + cap - 1) / cap, 0>(sm, ksb, tw, tws);
 }
 
 // Inverse levels R-1 .. l_stop of the tile in shared memory.
@@ -253,18 +257,20 @@ __device__ __forceinline__ void tile_inverse(u64* sm, int R, u64 ksb, const u64*
     __syncthreads();
   }
 }
-template <int C, int PR, int R, int LSTOP>
-__device__ __forceinline__ void tile_inverse_ct(u64* sm, u64 ksb, const u64* tw, const u64* tws) {
-  constexpr int cap = group_cap_ct(C, R);
-  constexpr int n = (R - LSTOP + cap - 1) / cap;
-  int l = R;
-#pragma unroll
-  for (int g = 0; g < n; ++g) {
-    const int k = (l - LSTOP + (n - g) - 1) / (n - g);
-    l -= k;
-    run_group<C, true, PR>(sm, k, l, R, ksb, tw, tws);
+// Inverse groups from level L (exclusive) down to LSTOP.
+template <int C, int PR, int R, int L, int LSTOP, int N, int G>
+__device__ __forceinline__ void inv_groups_ct(u64* sm, u64 ksb, const u64* tw, const u64* tws) {
+  if constexpr (G < N) {
+    constexpr int K = (L - LSTOP + (N - G) - 1) / (N - G);
+    level_group<K, C, true, PR>(sm, L - K, R, ksb, tw, tws);
     __syncthreads();
+    inv_groups_ct<C, PR, R, L - K, LSTOP, N, G + 1>(sm, ksb, tw, tws);
   }
+}
+template <int C, int PR, int R, int LSTOP, int MAXK = 3>
+__device__ __forceinline__ void tile_inverse_ct(u64* sm, u64 ksb, const u64* tw, const u64* tws) {
+  constexpr int cap = group_cap_ct(C, R, MAXK);
+  inv_groups_ct<C, PR, R, R, LSTOP, (R - LSTOP + cap - 1) / cap, 0>(sm, ksb, tw, tws);
 }
 
 // Forward levels [l0, R) / inverse levels R-1 .. l_stop: the compile-time
@@ -272,10 +278,10 @@ __device__ __forceinline__ void tile_inverse_ct(u64* sm, u64 ksb, const u64* tw,
 // passes of 7-9 levels, contiguous passes of 10-11), the runtime loop
 // otherwise.  Only the per-call kernels take them (CT); the batch kernel
 // keeps one code path per width.
-template <int C, int PR, bool CT>
+template <int C, int PR, bool CT, int MAXK = 3>
 __device__ __forceinline__ void tile_forward_any(u64* sm, int R, u64 ksb, const u64* tw, const u64* tws, int l0) {
   if constexpr (CT && C == 2) {
-    if (R == 11 && l0 == 0) return tile_forward_ct<C, PR, 11, 0>(sm, ksb, tw, tws);
+    if (R == 11 && l0 == 0) return tile_forward_ct<C, PR, 11, 0, MAXK>(sm, ksb, tw, tws);
     if (R == 10 && l0 == 0) return tile_forward_ct<C, PR, 10, 0>(sm, ksb, tw, tws);
   } else if constexpr (CT && C == 16) {
     if (R == 8 && l0 == 0) return tile_forward_ct<C, PR, 8, 0>(sm, ksb, tw, tws);
@@ -287,10 +293,10 @@ __device__ __forceinline__ void tile_forward_any(u64* sm, int R, u64 ksb, const 
   }
   tile_forward<C, PR>(sm, R, ksb, tw, tws, l0);
 }
-template <int C, int PR, bool CT>
+template <int C, int PR, bool CT, int MAXK = 3>
 __device__ __forceinline__ void tile_inverse_any(u64* sm, int R, u64 ksb, const u64* tw, const u64* tws, int l_stop) {
   if constexpr (CT && C == 2) {
-    if (R == 11 && l_stop == 0) return tile_inverse_ct<C, PR, 11, 0>(sm, ksb, tw, tws);
+    if (R == 11 && l_stop == 0) return tile_inverse_ct<C, PR, 11, 0, MAXK>(sm, ksb, tw, tws);
     if (R == 10 && l_stop == 0) return tile_inverse_ct<C, PR, 10, 0>(sm, ksb, tw, tws);
   } else if constexpr (CT && C == 16) {
     if (R == 8 && l_stop == 0) return tile_inverse_ct<C, PR, 8, 0>(sm, ksb, tw, tws);
@@ -327,7 +333,7 @@ __device__ __forceinline__ void pointwise4(u64 (&o)[4], const u64 (&A)[4], const
 // skip: the first `skip` local levels are not run (already done by the pass
 // before).  A contiguous tile of R levels with skip = w is 2^w consecutive
 // tiles of R - w levels, so small tiles can be worked on together.
-template <int C, bool FIRST, bool INV, bool SCALE, bool CG, bool FUSED, int PR>
+template <int C, bool FIRST, bool INV, bool SCALE, bool CG, bool FUSED, int PR, int MAXK = 3>
 __device__ __forceinline__ void pass_tile_p(u64* sm, const u64* in, u64* out, u64 n_in, int s, int lambda0, int R,
                                             const u64* __restrict__ tab, const u64* __restrict__ itab, u64 tab_stride,
                                             u64 tile, const u64* other, int skip) {
@@ -383,7 +389,7 @@ __device__ __forceinline__ void pass_tile_p(u64* sm, const u64* in, u64* out, u6
   __syncthreads();
 
   if (!INV) {
-    tile_forward_any<C, PR, !CG>(sm, R, ksb, tw, tws, half ? 1 : skip);
+    tile_forward_any<C, PR, !CG, MAXK>(sm, R, ksb, tw, tws, half ? 1 : skip);
     if (FUSED) {  // contiguous tile: smem index == position - base; other == nullptr squares
       const u64* oth = other ? other + (u64)PR * L : nullptr;
       const ulonglong2* twsv = reinterpret_cast<const ulonglong2*>(tws);
@@ -408,7 +414,7 @@ __device__ __forceinline__ void pass_tile_p(u64* sm, const u64* in, u64* out, u6
       stage_twiddles(tws, itw, ksb, R);
       cp_async_wait_all();
       __syncthreads();
-      tile_inverse_any<C, PR, !CG>(sm, R, ksb, itw, tws, skip);
+      tile_inverse_any<C, PR, !CG, MAXK>(sm, R, ksb, itw, tws, skip);
     }
   } else {
     tile_inverse_any<C, PR, !CG>(sm, R, ksb, tw, tws, skip);
@@ -426,20 +432,22 @@ __device__ __forceinline__ void pass_tile_p(u64* sm, const u64* in, u64* out, u6
   }
 }
 
-template <int C, bool FIRST, bool INV, bool SCALE, bool CG, bool FUSED = false>
+// MAXK: the largest register group (levels) the compile-time schedules may
+// use; 4 only where the kernel has the registers for 16 residues a thread.
+template <int C, bool FIRST, bool INV, bool SCALE, bool CG, bool FUSED = false, int MAXK = 3>
 __device__ __forceinline__ void pass_tile(u64* sm, const u64* in, u64* out, u64 n_in, int s, int lambda0, int R,
                                           const u64* __restrict__ tab, u64 tab_stride, int prime, u64 tile,
                                           const u64* __restrict__ itab = nullptr, const u64* other = nullptr,
                                           int skip = 0) {
   if (prime == 0)
-    pass_tile_p<C, FIRST, INV, SCALE, CG, FUSED, 0>(sm, in, out, n_in, s, lambda0, R, tab, itab, tab_stride, tile,
-                                                   other, skip);
+    pass_tile_p<C, FIRST, INV, SCALE, CG, FUSED, 0, MAXK>(sm, in, out, n_in, s, lambda0, R, tab, itab, tab_stride,
+                                                         tile, other, skip);
   else if (prime == 1)
-    pass_tile_p<C, FIRST, INV, SCALE, CG, FUSED, 1>(sm, in, out, n_in, s, lambda0, R, tab, itab, tab_stride, tile,
-                                                   other, skip);
+    pass_tile_p<C, FIRST, INV, SCALE, CG, FUSED, 1, MAXK>(sm, in, out, n_in, s, lambda0, R, tab, itab, tab_stride,
+                                                         tile, other, skip);
   else
-    pass_tile_p<C, FIRST, INV, SCALE, CG, FUSED, 2>(sm, in, out, n_in, s, lambda0, R, tab, itab, tab_stride, tile,
-                                                   other, skip);
+    pass_tile_p<C, FIRST, INV, SCALE, CG, FUSED, 2, MAXK>(sm, in, out, n_in, s, lambda0, R, tab, itab, tab_stride,
+                                                         tile, other, skip);
 }
 
 // Pointwise product of one group g (4 residues) of prime i.

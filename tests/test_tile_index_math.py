@@ -85,6 +85,28 @@ def test_level_groups_index_identity(C):
             check_group(C, R, l, K)
 
 
+def test_radix16_groups_of_11_level_contiguous_tiles():
+    """The compile-time schedule of 11-level contiguous tiles (C = 2) runs
+    4 + 4 + 3 levels forward and 4 + 4 + 3 back (tile_forward_ct /
+    tile_inverse_ct): 16-row units, one per thread."""
+    C, R = 2, 11
+    fwd, inv, l = [], [], 0
+    n = 3
+    for g in range(n):
+        k = (R - l + (n - g) - 1) // (n - g)
+        fwd.append((l, k))
+        l += k
+    l = R
+    for g in range(n):
+        k = (l + (n - g) - 1) // (n - g)
+        l -= k
+        inv.append((l, k))
+    assert fwd == [(0, 4), (4, 4), (8, 3)] and inv == [(7, 4), (3, 4), (0, 3)]
+    for l, K in fwd + inv:
+        assert (C << (R - K)) >= THREADS
+        check_group(C, R, l, K)
+
+
 def test_wide_tile_loads_aligned():
     """Pass loads copy pairs (idx, idx+1) with 16-byte copies: both the global
     position and the padded shared index must be even."""
