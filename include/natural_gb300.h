@@ -39,7 +39,10 @@ typedef struct nn_context nn_context;
 typedef struct nn_transform nn_transform;
 
 /* ---- context ------------------------------------------------------------ */
-/* Creates a context on `device`.  hbm_budget_bytes = 0 means no budget. */
+/* Creates a context on `device`.  hbm_budget_bytes = 0 means no budget.
+ * The tunables of the tuning file are applied to it (see
+ * nn_context_set_tunable): $NN_TUNING if set ("off": none), else the
+ * tuning.json the autotuner wrote beside the package. */
 nn_status nn_context_create(int device, uint64_t hbm_budget_bytes, nn_context** out);
 nn_status nn_context_destroy(nn_context* ctx);
 /* Order all work on a caller-owned cudaStream_t (NULL = the legacy default stream). */

@@ -3,9 +3,11 @@
 // ntt.cu / carry.cu on one CUDA stream; no computation happens on the host
 // besides size bookkeeping and the final normalisation of host results.
 #include <cuda_runtime.h>
+#include <dlfcn.h>
 
 #include <algorithm>
 #include <bit>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <map>
@@ -794,6 +796,51 @@ uint64_t nn_profile_report(char* buf, uint64_t cap) {
   return r.size();
 }
 
+// The tunables autotune.py measured on this GPU model (the "tunables" object
+// of tuning.json: "name": integer pairs), applied to every new context, so
+// that contexts made through the C ABI (the drop-in header's, the request
+// server's) run the same tuned pass splits and batch shapes as Python ones.
+// The file: $NN_TUNING ("off": none), else tuning.json in the directory above
+// the one holding this library.  A missing or unreadable file leaves the
+// defaults.
+static void apply_tuning_file(nn_context* c) {
+  std::string path;
+  if (const char* e = std::getenv("NN_TUNING")) {
+    if (std::strcmp(e, "off") == 0) return;
+    path = e;
+  } else {
+    Dl_info info{};
+    if (!dladdr(reinterpret_cast<void*>(&apply_tuning_file), &info) || !info.dli_fname) return;
+    std::string lib(info.dli_fname);
+    const size_t slash = lib.rfind('/');
+    const std::string dir = slash == std::string::npos ? "." : lib.substr(0, slash);
+    path = dir + "/../tuning.json";
+  }
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) return;
+  std::string text;
+  char buf[4096];
+  for (size_t n; (n = std::fread(buf, 1, sizeof buf, f)) > 0;) text.append(buf, n);
+  std::fclose(f);
+  size_t at = text.find("\"tunables\"");
+  if (at == std::string::npos) return;
+  at = text.find('{', at);
+  const size_t end = at == std::string::npos ? at : text.find('}', at);
+  if (end == std::string::npos) return;
+  for (size_t q = text.find('"', at); q != std::string::npos && q < end; q = text.find('"', q)) {
+    const size_t q2 = text.find('"', q + 1);
+    if (q2 == std::string::npos || q2 > end) break;
+    const std::string key = text.substr(q + 1, q2 - q - 1);
+    const size_t colon = text.find(':', q2);
+    if (colon == std::string::npos || colon > end) break;
+    char* stop = nullptr;
+    const long long v = std::strtoll(text.c_str() + colon + 1, &stop, 10);
+    if (stop != text.c_str() + colon + 1) nn_context_set_tunable(c, key.c_str(), v);
+    q = stop ? (size_t)(stop - text.c_str()) : colon + 1;
+  }
+  c->err.clear();  // an unknown key from another version is not an error of this context
+}
+
 nn_status nn_context_create(int device, uint64_t budget, nn_context** out) {
   if (!out) return NN_ERR_INVALID;
   *out = nullptr;
@@ -833,6 +880,7 @@ nn_status nn_context_create(int device, uint64_t budget, nn_context** out) {
     return st;
   }
   c->stream = c->own;
+  apply_tuning_file(c);
   *out = c;
   return NN_OK;
 }
