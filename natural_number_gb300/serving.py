@@ -71,23 +71,45 @@ def closed_loop(srv, W: ServeWorkload, window: int = 64) -> dict:
 
 def open_loop(srv, W: ServeWorkload, rate: float, seed: int = 4) -> dict:
     """Submits job k at its Poisson arrival time (rate jobs/s); latency is
-    completion minus arrival on the server's clock."""
+    completion minus arrival on the server's clock.  A second thread waits
+    for the results in submission order while the submissions go on, so a
+    result's buffer is released once it is read and a long stream does not
+    hold every product in host memory at once."""
+    import queue
+    import threading
+
     rng = np.random.default_rng(seed)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, len(W.jobs)))
-    tickets = []
+    tickets: queue.Queue = queue.Queue()
+    metas, errors = [], []
+
+    def consume():
+        while True:
+            t = tickets.get()
+            if t is None:
+                return
+            try:
+                metas.append(srv.wait(t)[1])
+            except Exception as e:  # reported after the stream; keep draining
+                errors.append(e)
+
+    waiter = threading.Thread(target=consume, daemon=True)
+    waiter.start()
     t0 = time.perf_counter()
-    for job, at in zip(W.jobs, arrivals):
-        delay = at - (time.perf_counter() - t0)
-        if delay > 0:
-            time.sleep(delay)
-        tickets.append(_submit(srv, job))
-    lat, t_first, t_last = [], None, 0.0
-    for t in tickets:
-        _, meta = srv.wait(t)
-        lat.append(meta["done"] - meta["submit"])
-        t_first = meta["submit"] if t_first is None else min(t_first, meta["submit"])
-        t_last = max(t_last, meta["done"])
-    lat = np.array(lat)
+    try:
+        for job, at in zip(W.jobs, arrivals):
+            delay = at - (time.perf_counter() - t0)
+            if delay > 0:
+                time.sleep(delay)
+            tickets.put(_submit(srv, job))
+    finally:
+        tickets.put(None)
+        waiter.join()
+    if errors:
+        raise errors[0]
+    lat = np.array([m["done"] - m["submit"] for m in metas])
+    t_first = min(m["submit"] for m in metas)
+    t_last = max(m["done"] for m in metas)
     return {"rate_jobs_per_s": rate, "p50_ms": float(np.percentile(lat, 50) * 1e3),
             "p99_ms": float(np.percentile(lat, 99) * 1e3), "mean_ms": float(lat.mean() * 1e3),
             "limbs_per_s": W.limbs_total / (t_last - t_first)}
