@@ -350,7 +350,7 @@ def main() -> None:
     ap.add_argument("--no-batch", action="store_true", help="skip the uneven-size batch measurement")
     ap.add_argument("--batch-count", type=int, default=4096, help="products in the uneven-size batch")
     ap.add_argument("--no-serve", action="store_true", help="skip the served request stream")
-    ap.add_argument("--serve-jobs", type=int, default=1000)
+    ap.add_argument("--serve-jobs", type=int, default=5000)
     ap.add_argument("--no-series", action="store_true", help="skip pi and e to 10^8 digits (a few seconds)")
     ap.add_argument("--no-div", action="store_true", help="skip the 2^22 / 2^21-limb division")
     args = ap.parse_args()
