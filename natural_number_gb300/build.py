@@ -23,7 +23,8 @@ NVCC = shutil.which("nvcc") or os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["ntt.cu", "carry.cu", "batch.cu", "noalloc.cu"]
-CPP_SOURCES = ["engine.cpp", "profile.cpp", "natural_ops.cpp", "serve.cpp", "series.cpp", "host_glue.cpp", "divide.cpp"]
+CPP_SOURCES = ["engine.cpp", "profile.cpp", "natural_ops.cpp", "serve.cpp", "series.cpp", "host_glue.cpp", "divide.cpp",
+               "host_pool.cpp"]
 HEADERS = ["nn_device.cuh", "nn_internal.h", "ntt_tiles.cuh", "scan_tiles.cuh", "context_access.h",
            "../../include/natural_gb300.hpp"]
 
