@@ -306,6 +306,9 @@ def _ref_worker(args):
     return time.perf_counter() - t0
 
 
+REF_N_EXP = 23
+
+
 def run_reference(args) -> None:
     """CPU reference arm: the oracle restatement (the reference's x86-64
     assembly does not build on this Arm host), one independent product per
@@ -317,7 +320,7 @@ def run_reference(args) -> None:
     from oracle import build_oracle
     build_oracle()
     cores = os.cpu_count() or 1
-    n = 1 << 22
+    n = 1 << REF_N_EXP
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores) as pool:
         for w in range(args.warmup):
@@ -327,15 +330,100 @@ def run_reference(args) -> None:
             pool.map(_ref_worker, [(n, 17 + 2 * i) for i in range(cores)])
         dt = (time.perf_counter() - t0) / args.steps
     value = cores * 2 * n / dt
+    sample = "%d independent 2^%d x 2^%d-limb products per step, one per host core" % (cores, REF_N_EXP, REF_N_EXP)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic (SplitMix64)",
-            "config": {"workload": "plain multiply, sampled: %d independent 2^22 x 2^22-limb products per step "
-                                   "(one per host core) standing in for one 2^27 x 2^27 product" % cores},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": "%d x (2^22 x 2^22) per step" % cores},
+            "config": {"workload": "plain multiply, sampled: %s, standing in for one 2^27 x 2^27 product" % sample},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line))
+    print(json.dumps(line), flush=True)
+
+
+class Legs:
+    """Progress and deadlines of the bench's legs.
+
+    Every leg writes a timestamped start and end line to stderr.  A watchdog
+    thread holds each leg to a wall-clock budget and the whole run to a total
+    one.  A leg that raises is recorded under "skipped" and the run goes on;
+    a leg that overruns its budget is recorded the same way, the result line
+    gathered so far is printed, and the process ends, since a thread stuck in
+    native code cannot be stopped from Python.  Legs that would start after
+    the total budget is spent are recorded as not run."""
+
+    def __init__(self, line: dict, total_s: float):
+        import threading
+        self.t0 = time.perf_counter()
+        self.total_end = self.t0 + total_s
+        self.line = line
+        self.lock = threading.Lock()
+        self.current = None
+        self.printed = False
+        self.core_done = False
+        threading.Thread(target=self._watch, daemon=True).start()
+
+    def log(self, msg: str) -> None:
+        sys.stderr.write("[bench %7.1f s] %s\n" % (time.perf_counter() - self.t0, msg))
+        sys.stderr.flush()
+
+    def skip(self, name: str, why: str) -> None:
+        with self.lock:
+            self.line.setdefault("skipped", {})[name] = why
+        self.log("skipped %s: %s" % (name, why))
+
+    def run(self, name: str, budget_s: float, fn, core: bool = False):
+        """fn() under the leg's budget; its result, or None if it was skipped."""
+        now = time.perf_counter()
+        if not core and now + budget_s > self.total_end:
+            self.skip(name, "not run: the bench's total time budget would be exceeded")
+            return None
+        with self.lock:
+            self.current = (name, now + budget_s, budget_s)
+        self.log("start %s (budget %.0f s)" % (name, budget_s))
+        try:
+            out = fn()
+        except Exception as e:  # noqa: BLE001 - a failed leg is reported in the line
+            with self.lock:
+                self.current = None
+            if core:
+                raise
+            self.skip(name, "failed: %s: %s" % (type(e).__name__, str(e)[:300]))
+            return None
+        with self.lock:
+            self.current = None
+        self.log("done %s in %.1f s" % (name, time.perf_counter() - now))
+        return out
+
+    def emit(self) -> None:
+        with self.lock:
+            if self.printed:
+                return
+            self.printed = True
+            text = json.dumps(self.line)
+        sys.stdout.write(text + "\n")
+        sys.stdout.flush()
+
+    def _watch(self) -> None:
+        while True:
+            time.sleep(0.5)
+            with self.lock:
+                cur = self.current
+            if cur is None or time.perf_counter() <= cur[1]:
+                continue
+            name, _, budget = cur
+            self.skip(name, "timed out after its %.0f s budget; the run was ended there" % budget)
+            if self.core_done:
+                self.emit()
+            self._exit(0 if self.core_done else 1)
+
+    def _exit(self, code: int) -> None:
+        """Runs the interpreter's exit handlers (bounded) and ends the process."""
+        import atexit
+        import threading
+        t = threading.Thread(target=atexit._run_exitfuncs, daemon=True)
+        t.start()
+        t.join(10.0)
+        os._exit(code)
 
 
 def main() -> None:
@@ -350,21 +438,28 @@ def main() -> None:
     ap.add_argument("--no-batch", action="store_true", help="skip the uneven-size batch measurement")
     ap.add_argument("--batch-count", type=int, default=4096, help="products in the uneven-size batch")
     ap.add_argument("--no-serve", action="store_true", help="skip the served request stream")
-    ap.add_argument("--serve-jobs", type=int, default=5000)
+    ap.add_argument("--serve-jobs", type=int, default=4000)
+    ap.add_argument("--serve-rates", default="0.3,0.5,0.7,0.9",
+                    help="open-loop arrival rates as fractions of the measured capacity")
     ap.add_argument("--no-series", action="store_true", help="skip pi and e to 10^8 digits (a few seconds)")
     ap.add_argument("--no-div", action="store_true", help="skip the 2^22 / 2^21-limb division")
+    ap.add_argument("--total-budget", type=float, default=1200.0, help="seconds for the whole run")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
         return
 
-    import numpy as np
+    line: dict = {"metric": METRIC, "unit": UNIT, "steps": args.steps, "warmup": args.warmup,
+                  "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+                  "data": "synthetic (SplitMix64 uniform u64 limbs, top limb nonzero)"}
+    legs = Legs(line, args.total_budget)
+
     import torch
 
     import natural_number_gb300 as nn
+    from natural_number_gb300 import replicas
     from natural_number_gb300.synth import limbs
 
-    from natural_number_gb300 import replicas
     R = replicas.Rank.from_env()
     world, rank, local = R.world, R.rank, R.local
     torch.cuda.set_device(local)
@@ -375,50 +470,88 @@ def main() -> None:
 
     n = 1 << args.n_exp
     L = 1 << (args.n_exp + 1)
-    ctx = nn.Context(local)
-    stream = torch.cuda.current_stream()
-    seed_a, seed_b = R.seeds(SEED_A, SEED_B)
-    a = limbs(seed_a, n)
-    b = limbs(seed_b, n)
-    da = torch.from_numpy(a).to("cuda")
-    db = torch.from_numpy(b).to("cuda")
-    out = torch.empty(2 * n, dtype=torch.uint64, device="cuda")
+    st: dict = {}
 
-    for _ in range(max(args.warmup, 3)):
-        ctx.mul_device(out, da, db)
-    torch.cuda.synchronize()
+    def setup():
+        st["ctx"] = nn.Context(local)
+        seed_a, seed_b = R.seeds(SEED_A, SEED_B)
+        st["a"], st["b"] = limbs(seed_a, n), limbs(seed_b, n)
+        st["da"] = torch.from_numpy(st["a"]).to("cuda")
+        st["db"] = torch.from_numpy(st["b"]).to("cuda")
+        st["out"] = torch.empty(2 * n, dtype=torch.uint64, device="cuda")
+        for _ in range(max(args.warmup, 3)):
+            st["ctx"].mul_device(st["out"], st["da"], st["db"])
+        torch.cuda.synchronize()
+
+    legs.run("setup", 300, setup, core=True)
+    ctx, stream = st["ctx"], torch.cuda.current_stream()
     replicas.barrier(dist)
 
-    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    l0 = nn.launch_count()
-    nn.profile_enable(True)
-    with ClockSampler(local) as clk:
-        torch.cuda.synchronize()
-        start.record(stream)
-        for _ in range(args.steps):
-            ctx.mul_device(out, da, db)
-        stop.record(stream)
-        torch.cuda.synchronize()
-    nn.profile_enable(False)
-    prof = nn.profile_report()
-    launches = (nn.launch_count() - l0) / args.steps
-    ms = start.elapsed_time(stop) / args.steps
-    ctx.synchronize()
-    ms = replicas.max_over_ranks(ms, dist, "cuda")
-    replicas.barrier(dist)
+    def multiply():
+        start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = nn.launch_count()
+        nn.profile_enable(True)
+        with ClockSampler(local) as clk:
+            torch.cuda.synchronize()
+            start.record(stream)
+            for _ in range(args.steps):
+                ctx.mul_device(st["out"], st["da"], st["db"])
+            stop.record(stream)
+            torch.cuda.synchronize()
+        nn.profile_enable(False)
+        prof = nn.profile_report()
+        launches = (nn.launch_count() - l0) / args.steps
+        ms = start.elapsed_time(stop) / args.steps
+        ctx.synchronize()
+        ms = replicas.max_over_ranks(ms, dist, "cuda")
+        replicas.barrier(dist)
+        # spot-check the last product with size-independent modular identities
+        from tests.gpu_util import mod_checks
+        prod = st["out"].cpu().numpy()
+        ma, mb, mp = mod_checks(st["a"]), mod_checks(st["b"]), mod_checks(prod)
+        exact = mp[0] == ma[0] * mb[0] % (2**64 - 1) and mp[1] == ma[1] * mb[1] % (2**64 + 1)
+        return ms, prof, launches, clk.summary(), bool(exact)
+
+    ms, prof, launches, clocks, exact = legs.run("multiply", 180, multiply, core=True)
     value = replicas.aggregate_rate(2 * n, world, ms)
+    peak, peak_kind = peaks()
+    dname, (dcount, dms) = max(prof.items(), key=lambda kv: kv[1][1])
+    d_avg = dms / dcount
+    d_bytes = kernel_bytes(dname, n, n, L)
+    achieved = d_bytes / (d_avg / 1e3) / 1e9
+    mul_bytes = mul_algorithmic_bytes(n, n, L)
+    line.update({
+        "value": value, "n_gpus": world, "ms_per_step": ms,
+        "config": {"workload": "plain multiply, 2^%d x 2^%d limbs (%d MiB per operand), product %d limbs"
+                               % (args.n_exp, args.n_exp, n * 8 >> 20, 2 * n),
+                   "l2": "inputs larger than L2 (operands %d MiB, residues %d MiB per transform); no flush"
+                         % (n * 8 >> 20, 24 * L >> 20),
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "bit_exact_spot_check": exact},
+        "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": measured_traffic(dname, L), "peak_kind": peak_kind,
+                     "bytes_per_launch": d_bytes, "launch_ms": d_avg, "launches_per_step": dcount / args.steps},
+        "mul_roofline": {"algorithmic_bytes": mul_bytes, "achieved": mul_bytes / (ms / 1e3) / 1e9,
+                         "frac": mul_bytes / (ms / 1e3) / 1e9 / peak, "peak_kind": peak_kind},
+        "kernels": {k: {"launches_per_step": c / args.steps, "ms_per_step": t / args.steps}
+                    for k, (c, t) in prof.items()},
+        "gpu_launches": launches, "clocks": clocks})
+    # The passes are bound by integer issue as much as by HBM: one warp
+    # instruction per scheduler (4 per SM) per cycle at the sampled SM clock
+    # is the issue peak.
+    inst = measured_instructions(dname, L)
+    if inst and clocks.get("sm_mhz"):
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        ipeak = 4.0 * sms * clocks["sm_mhz"] * 1e6
+        iach = inst / (d_avg / 1e3)
+        line["issue_roofline"] = {"bound": "int_issue", "kernel": dname, "achieved": iach, "peak": ipeak,
+                                  "unit": "warp inst/s", "frac": iach / ipeak, "inst_per_launch": inst,
+                                  "source": "profiles/instructions.txt (ncu on a smaller transform, scaled by L); "
+                                            "peak 4 per SM per cycle"}
 
-    # spot-check the last product with size-independent modular identities
-    prod = out.cpu().numpy()
-    from tests.gpu_util import mod_checks
-    ma, mb, mp = mod_checks(a), mod_checks(b), mod_checks(prod)
-    exact = mp[0] == ma[0] * mb[0] % (2**64 - 1) and mp[1] == ma[1] * mb[1] % (2**64 + 1)
-    del prod
-
-    e2e = None
-    if not args.no_e2e:
-        ha = torch.from_numpy(a).pin_memory().numpy()
-        hb = torch.from_numpy(b).pin_memory().numpy()
+    def e2e():
+        ha = torch.from_numpy(st["a"]).pin_memory().numpy()
+        hb = torch.from_numpy(st["b"]).pin_memory().numpy()
         ho = torch.empty(2 * n, dtype=torch.uint64).pin_memory().numpy()
         for _ in range(2):
             ctx.mul(ha, hb, out=ho)
@@ -433,81 +566,52 @@ def main() -> None:
         e_ms = replicas.max_over_ranks(e_ms, dist, "cuda")
         # value: the mean over the K steps; the spread shows host-side stalls
         # (the host link and memory are shared with other jobs on the machine)
-        e2e = {"value": replicas.aggregate_rate(2 * n, world, e_ms), "unit": UNIT, "ms_per_step": e_ms,
-               "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 16 * n,
-               "step_ms_median": statistics.median(step_ms), "step_ms_min": min(step_ms),
-               "step_ms_max": max(step_ms)}
+        return {"value": replicas.aggregate_rate(2 * n, world, e_ms), "unit": UNIT, "ms_per_step": e_ms,
+                "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 16 * n,
+                "api": "nn_mul_host (page-locked host operands in, product out, every step)",
+                "step_ms_median": statistics.median(step_ms), "step_ms_min": min(step_ms),
+                "step_ms_max": max(step_ms)}
 
-    square = measure_square(ctx, da, n, args.steps, args.warmup)
-    division = measure_division(ctx, cpu=not args.no_cpu) if rank == 0 and not args.no_div else None
+    if not args.no_e2e:
+        r = legs.run("e2e", 180, e2e, core=True)
+        line["e2e"] = r
+    if rank == 0 and not args.no_cpu:
+        r = legs.run("cpu_baseline", 240, cpu_baseline_port, core=True)
+        line["cpu_baseline"] = r
+    legs.core_done = True
 
-    batched = None
+    r = legs.run("square", 120, lambda: measure_square(ctx, st["da"], n, args.steps, args.warmup))
+    if r:
+        line["square"] = r
+    del st["db"]
     if not args.no_batch:
-        batched = measure_batched(ctx, args.steps, args.warmup, args.batch_count)
-    serving = None
-    if not args.no_serve and rank == 0:
+        r = legs.run("batched", 240, lambda: measure_batched(ctx, args.steps, args.warmup, args.batch_count))
+        if r:
+            line["batched"] = r
+    if rank == 0 and not args.no_serve:
         from natural_number_gb300 import serving as serving_mod
-        serving = serving_mod.measure(args.serve_jobs)
+        rates = tuple(float(x) for x in args.serve_rates.split(",") if x)
+        r = legs.run("serving", 420, lambda: serving_mod.measure(args.serve_jobs, rates))
+        if r:
+            line["serving"] = r
+    if rank == 0 and not args.no_series:
+        r = legs.run("series", 240, lambda: measure_series(ctx))
+        if r:
+            line["series"] = r
+    if rank == 0 and not args.no_div:
+        r = legs.run("division", 180, lambda: measure_division(ctx, cpu=not args.no_cpu))
+        if r:
+            line["division"] = r
 
-    series = measure_series(ctx) if not args.no_series and rank == 0 else None
+    if rank == 0:
+        legs.emit()
 
-    if rank != 0:
-        return
-    peak, peak_kind = peaks()
-    dom = max(prof.items(), key=lambda kv: kv[1][1])
-    dname, (dcount, dms) = dom
-    d_avg = dms / dcount
-    d_bytes = kernel_bytes(dname, n, n, L)
-    achieved = d_bytes / (d_avg / 1e3) / 1e9
-    traffic = measured_traffic(dname, L)
-    mul_bytes = mul_algorithmic_bytes(n, n, L)
-    clocks = clk.summary()
-    # The kernels are bound by integer issue, not HBM: one warp instruction
-    # per scheduler (4 per SM) per cycle at the sampled SM clock is the peak.
-    inst = measured_instructions(dname, L)
-    issue = None
-    if inst and clocks.get("sm_mhz"):
-        sms = torch.cuda.get_device_properties(local).multi_processor_count
-        ipeak = 4.0 * sms * clocks["sm_mhz"] * 1e6
-        iach = inst / (d_avg / 1e3)
-        issue = {"bound": "int_issue", "kernel": dname, "achieved": iach, "peak": ipeak, "unit": "warp inst/s",
-                 "frac": iach / ipeak, "inst_per_launch": inst,
-                 "source": "profiles/instructions.txt (ncu at L = 2^23, scaled by L); peak 4 per SM per cycle"}
-    line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
-        "data": "synthetic (SplitMix64 uniform u64 limbs, top limb nonzero)",
-        "config": {"workload": "plain multiply, 2^%d x 2^%d limbs (%d MiB per operand), product %d limbs"
-                               % (args.n_exp, args.n_exp, n * 8 >> 20, 2 * n),
-                   "l2": "inputs larger than L2 (operands %d MiB, residues %d MiB per transform); no flush"
-                         % (n * 8 >> 20, 24 * L >> 20),
-                   "parallelism": "replicas" if world > 1 else "single GPU",
-                   "bit_exact_spot_check": bool(exact)},
-        "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                     "bytes_per_launch": d_bytes, "launch_ms": d_avg, "launches_per_step": dcount / args.steps},
-        "mul_roofline": {"algorithmic_bytes": mul_bytes, "achieved": mul_bytes / (ms / 1e3) / 1e9,
-                         "frac": mul_bytes / (ms / 1e3) / 1e9 / peak},
-        "kernels": {k: {"launches_per_step": c / args.steps, "ms_per_step": t / args.steps} for k, (c, t) in prof.items()},
-        "gpu_launches": launches,
-        "clocks": clocks,
-    }
-    if issue:
-        line["issue_roofline"] = issue
-    line["square"] = square
-    if division:
-        line["division"] = division
-    if e2e:
-        line["e2e"] = e2e
-    if series:
-        line["series"] = series
-    if batched:
-        line["batched"] = batched
-    if serving:
-        line["serving"] = serving
-    if not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline_port()
-    print(json.dumps(line))
+    def teardown():
+        st.clear()
+        ctx.close()
+        torch.cuda.synchronize()
+
+    legs.run("teardown", 60, teardown, core=True)
 
 
 if __name__ == "__main__":

@@ -206,7 +206,9 @@ nn_status nn_server_submit_mul(nn_server* s, const uint64_t* a, uint64_t n_a, co
 /* q: n_a + 1 limbs, r: max(n_a, n_b) + 1 limbs (the reference's result sizes fit). */
 nn_status nn_server_submit_div(nn_server* s, const uint64_t* a, uint64_t n_a, const uint64_t* b, uint64_t n_b,
                                uint64_t* q, uint64_t* r, uint64_t* ticket);
-/* Waits for a request (NN_ERR_TIMEOUT after timeout_s), fills info, forgets the ticket. */
+/* Waits for a request, fills info and forgets the ticket.  After timeout_s
+ * it returns NN_ERR_TIMEOUT instead: the request is still queued or in
+ * flight, its host buffers are still in use, and the ticket stays valid. */
 nn_status nn_server_wait(nn_server* s, uint64_t ticket, double timeout_s, nn_request_info* info);
 nn_status nn_server_get_stats(nn_server* s, nn_server_stats* out);
 double nn_server_clock(nn_server* s);

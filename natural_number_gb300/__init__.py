@@ -516,10 +516,17 @@ class Server:
         self._keep[t.value] = ("div", a, b, q, r)
         return t.value
 
-    def wait(self, ticket: int, timeout: float = 600.0):
-        """Returns (result, info): the product, or (quotient, remainder)."""
+    def wait(self, ticket: int, timeout: float = 30.0):
+        """Returns (result, info): the product, or (quotient, remainder).
+
+        Raises NNError with NN_ERR_TIMEOUT if the request has not finished
+        within `timeout` seconds; the request stays queued or in flight, its
+        host buffers stay referenced here, and the ticket can be waited on
+        again."""
         info = RequestInfo()
         st = lib().nn_server_wait(self.h, ticket, timeout, C.byref(info))
+        if st == NN_ERR_TIMEOUT:
+            raise NNError(st, "request %d not finished within %.1f s" % (ticket, timeout))
         kind, _, _, out, r = self._keep.pop(ticket)
         if st != NN_OK:
             raise NNError(st, "request failed: " + lib().nn_status_string(st).decode())

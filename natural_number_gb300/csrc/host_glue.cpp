@@ -23,6 +23,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <functional>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -54,6 +55,12 @@ unsigned usable_cores() {
 // Persistent workers; one parallel operation at a time (a caller that finds
 // the pool busy runs its operation alone).  Never destroyed: the workers
 // outlive static destruction.
+//
+// Each operation is a Job of its own with its own task and completion
+// counters, shared by reference count.  A worker that wakes for one job but
+// reaches it only after the job has finished (and the next has started)
+// still holds the old job: it finds every task claimed and goes back to
+// sleep, and never claims or counts a task of the newer job.
 class Pool {
  public:
   static Pool& get() {
@@ -66,54 +73,67 @@ class Pool {
   bool run(unsigned tasks, const std::function<void(unsigned)>& f) {
     std::unique_lock<std::mutex> busy(run_mu_, std::try_to_lock);
     if (!busy.owns_lock()) return false;
+    auto job = std::make_shared<Job>(f, tasks);
     {
       std::lock_guard<std::mutex> g(mu_);
-      job_ = &f;
-      tasks_ = tasks;
-      next_.store(0);
-      left_.store(tasks);
+      job_ = job;
       ++gen_;
     }
     cv_.notify_all();
-    work();
-    std::unique_lock<std::mutex> g(mu_);
-    done_cv_.wait(g, [&] { return left_.load() == 0; });
-    job_ = nullptr;
+    work(*job);
+    {
+      std::unique_lock<std::mutex> g(job->mu);
+      job->done_cv.wait(g, [&] { return job->left.load() == 0; });
+    }
+    std::lock_guard<std::mutex> g(mu_);
+    job_.reset();  // workers still inside work() keep their own reference
     return true;
   }
 
  private:
+  struct Job {
+    Job(const std::function<void(unsigned)>& f_, unsigned tasks_) : f(f_), tasks(tasks_), left(tasks_) {}
+    const std::function<void(unsigned)>& f;  // lives in run()'s caller until every task is counted
+    const unsigned tasks;
+    std::atomic<unsigned> next{0}, left;
+    std::mutex mu;
+    std::condition_variable done_cv;
+  };
+
   Pool() : n_(usable_cores()) {
     for (unsigned t = 1; t < n_; ++t) std::thread([this] { loop(); }).detach();
   }
-  void work() {
+  // Claims and runs tasks of `J` until none is left.  f is touched only for
+  // a claimed task, and run() returns only after every claimed task is
+  // counted, so f outlives every use.
+  static void work(Job& J) {
     for (;;) {
-      const unsigned k = next_.fetch_add(1);
-      if (k >= tasks_) return;
-      (*job_)(k);
-      if (left_.fetch_sub(1) == 1) {
-        std::lock_guard<std::mutex> g(mu_);
-        done_cv_.notify_all();
+      const unsigned k = J.next.fetch_add(1);
+      if (k >= J.tasks) return;
+      J.f(k);
+      if (J.left.fetch_sub(1) == 1) {
+        std::lock_guard<std::mutex> g(J.mu);
+        J.done_cv.notify_all();
       }
     }
   }
   void loop() {
     unsigned long long seen = 0;
     for (;;) {
+      std::shared_ptr<Job> J;
       {
         std::unique_lock<std::mutex> g(mu_);
         cv_.wait(g, [&] { return gen_ != seen && job_ != nullptr; });
         seen = gen_;
+        J = job_;
       }
-      work();
+      work(*J);
     }
   }
   const unsigned n_;
   std::mutex run_mu_, mu_;
-  std::condition_variable cv_, done_cv_;
-  const std::function<void(unsigned)>* job_ = nullptr;
-  unsigned tasks_ = 0;
-  std::atomic<unsigned> next_{0}, left_{0};
+  std::condition_variable cv_;
+  std::shared_ptr<Job> job_;
   unsigned long long gen_ = 0;
 };
 

@@ -93,3 +93,37 @@ def test_copy():
     x = np.concatenate([s, np.zeros(7, dtype=np.uint64)])
     L.nn_host_copy(P(x, 7), P(x), n)  # overlapping: memmove
     assert np.array_equal(x[7:], s)
+
+
+def test_pool_shared_by_many_threads():
+    """Several host threads use the worker pool at once, many times over
+    (as the request server's scheduler, its division workers and the caller
+    do): every operation still completes, with the sequential results.  An
+    in-place shift is not idempotent, so a task run twice or counted in the
+    wrong operation shows up as a wrong value; a lost completion shows up as
+    a thread that does not finish."""
+    import threading
+    L = lib()
+    n = 1 << 16
+    errors, done = [], []
+
+    def worker(t):
+        s = limbs(100 + t, n)
+        want_shl = val(s) << 13
+        for it in range(150):
+            x = np.concatenate([s, np.zeros(1, dtype=np.uint64)])
+            L.nn_host_shl_n(13, n, P(x), P(x))
+            d = np.empty(n, dtype=np.uint64)
+            L.nn_host_copy(P(d), P(s), n)
+            if val(x) != want_shl or not np.array_equal(d, s):
+                errors.append((t, it))
+                return
+        done.append(t)
+
+    ts = [threading.Thread(target=worker, args=(t,), daemon=True) for t in range(6)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join(120)
+    assert not errors, errors
+    assert sorted(done) == list(range(6)), "a pool operation did not complete"
