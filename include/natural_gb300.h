@@ -171,12 +171,19 @@ int64_t nn_context_get_tunable(const nn_context* ctx, const char* name);
  * device.  Same product as nn_mul_base (d_out: n_a + n_b limbs, not
  * normalised), ordered on `stream` (a cudaStream_t; NULL = default stream),
  * without a context and without any allocation: the carry scan's status words
- * live in a fixed device array of the library, sized for n_a + n_b <= 2^22
- * limbs (larger products return NN_ERR_INVALID).  The first call on a device
- * looks up that array's device address (cudaGetSymbolAddress) with the device
- * current; make that first call before any stream capture.  Every call shares
- * the one array and clears what it needs, so calls that overlap on the GPU
- * (different streams, or devices sharing none of this) race: order them. */
+ * live in a fixed device array of the library (2^11 + 8 32-bit words per
+ * device), sized for n_a + n_b <= 2^22 limbs (larger products return
+ * NN_ERR_INVALID).  The first call on a device looks up that array's device
+ * address (cudaGetSymbolAddress) with the device current and keeps it; make
+ * that first call before any stream capture, and do not use the entry point
+ * after cudaDeviceReset on that device.  The call returns once the product is
+ * complete (it reads the scan's error word back and waits for `stream`):
+ * NN_ERR_TIMEOUT means a carry wait gave up and d_out is not the product.
+ * Every call on a device shares that device's array and clears what it needs,
+ * so calls that overlap on the GPU of one device race: order them (each
+ * device has its own array).  Test hook: NN_NOALLOC_SKIP_FIRST_TILE=1 in the
+ * environment leaves one status word unset, so a carry wait runs out and the
+ * call returns NN_ERR_TIMEOUT. */
 nn_status nn_mul_base_noalloc(const uint64_t* d_a, uint64_t n_a, const uint64_t* d_b, uint64_t n_b,
                               uint64_t* d_out, void* stream);
 
