@@ -1,6 +1,6 @@
 // carry.cu — multiword carry propagation on sm_103a: CRT recombination fused
-// with a decoupled-lookback carry scan, plus the same scan driving the
-// schoolbook base case and shifted multiword adds.
+// with a carry scan, plus the same scan driving the schoolbook base case and
+// shifted multiword adds.
 //
 // Each position k contributes a three-word value x_k (< 2^186) at limb k; the
 // output is sum_k x_k * B^k, B = 2^64 (asmCRT, asmLinux.asm:1369-1450, does
@@ -9,10 +9,21 @@
 // with a zero carry-in (H_t: two words).  Adding the neighbour's H_{t-1} into
 // lo_t leaves an E-limb value u_t plus a one-bit generate g_t; the remaining
 // carries are one bit each (propagate p_t = u_t is all ones; g_t and p_t are
-// exclusive), resolved by warp ballots inside a tile and by a decoupled
-// lookback on one status word per tile across tiles.  Tile ids come from an
-// atomic counter so every predecessor of a tile is already resident; each
-// wait is bounded and records an error instead of hanging.
+// exclusive), resolved by warp ballots inside a tile.
+//
+// Between tiles the per-call scans of more than 1024 tiles take three
+// launches and never wait:
+//  1. every tile runs with carry-in 0, writes its limbs and records its
+//     one-bit generate and propagate (no tile waits for another);
+//  2. one CTA composes those bits over the tiles (a scan of the maps
+//     carry-in -> carry-out) and records each tile's carry-in;
+//  3. each tile whose carry-in is 1 adds it at its first limb, where it
+//     ripples only while limbs wrap to zero.
+// Smaller per-call scans, the persistent batch kernel and the
+// allocation-free entry point take the decoupled lookback instead (scan_tile
+// with LOOKBACK: one launch, each tile's carry-in from its predecessors'
+// status words), whose waits are bounded and record an error instead of
+// hanging.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -28,17 +39,110 @@ NN_DEFINE_PRIME_UPLOADER(upload_primes_carry)
 
 namespace {
 
-// Per-call scan: tile ids come from an atomic counter (from tile_base), so
-// every predecessor of a tile has started before it, in this launch or in an
-// earlier one on the stream.
+// Scans of at most kLookbackTiles tiles take one launch: tile ids come from
+// an atomic counter (from tile_base), so every predecessor of a tile has
+// started before it, and each tile takes its carry-in by the decoupled
+// lookback.  Their tiles fit in one or two waves, so a lookback waits about
+// one tile's work; larger scans take the three steps below, which never wait.
+constexpr u64 kLookbackTiles = 1024;
 template <class Prod>
-__global__ void __launch_bounds__(kScanThreads, 3) scan_kernel(Prod prod, u64 total, u64* out, u64 out_limit,
-                                                            u64* side, u32* flags, u32* counter, u32* err,
-                                                            u32 tile_base) {
+__global__ void __launch_bounds__(kScanThreads, 3) scan_lookback_kernel(Prod prod, u64 total, u64* out, u64 out_limit,
+                                                                     u64* side, u32* flags, u32* counter, u32* err,
+                                                                     u32 tile_base) {
   __shared__ u32 s_tile;
   if (threadIdx.x == 0) s_tile = tile_base + atomicAdd(counter, 1u);
   __syncthreads();
   scan_tile(prod, s_tile, total, out, out_limit, side, flags, err);
+}
+
+// Step 1: tile tile_base + blockIdx.x with carry-in 0; flags[tile] receives
+// its generate (bit 0) and propagate (bit 1) bits.
+template <class Prod>
+__global__ void __launch_bounds__(kScanThreads, 3) scan_kernel(Prod prod, u64 total, u64* out, u64 out_limit,
+                                                            u64* side, u32* flags, u64 tile_base) {
+  scan_tile<Prod, false>(prod, tile_base + blockIdx.x, total, out, out_limit, side, flags, nullptr);
+}
+
+// Step 2: the carries between tiles [t0, t1), in chunks of kCarryChunk
+// tiles.  The chunk's status words come into shared memory with coalesced
+// loads; each thread folds kCarryPer consecutive tiles into the map carry-in
+// -> carry-out (the pair of outputs for carry-in 0 and 1); a scan over the
+// threads composes the maps; each thread walks its tiles again and sets bit 2
+// to the tile's carry-in; the words go back with coalesced stores.  The
+// carry into t0 is *chain (left there by the previous range of the same
+// scan) or 0 when t0 = 0; the carry out of t1 - 1 is left in *chain.
+constexpr int kCarryThreads = 1024, kCarryPer = 32, kCarryChunk = kCarryThreads * kCarryPer;
+__global__ void __launch_bounds__(kCarryThreads) tile_carry_kernel(u32* flags, u64 t0, u64 t1, u32* chain) {
+  __shared__ unsigned char sb[kCarryChunk];
+  __shared__ unsigned char m0[kCarryThreads], m1[kCarryThreads];
+  __shared__ u32 s_carry;
+  const int j = threadIdx.x;
+  if (j == 0) s_carry = t0 > 0 ? *chain : 0u;
+  for (u64 c0 = t0; c0 < t1; c0 += kCarryChunk) {
+    const u64 n = min((u64)kCarryChunk, t1 - c0);
+#pragma unroll 8
+    for (int i = 0; i < kCarryPer; ++i) {
+      const u64 k = (u64)i * kCarryThreads + j;
+      sb[k] = k < n ? (unsigned char)flags[c0 + k] : 2;  // past the range: propagates (the identity map)
+    }
+    __syncthreads();
+    u32 f0 = 0, f1 = 1;
+#pragma unroll 8
+    for (int i = 0; i < kCarryPer; ++i) {
+      const u32 v = sb[j * kCarryPer + i], g = v & 1, p = (v >> 1) & 1;
+      f0 = g | (p & f0);
+      f1 = g | (p & f1);
+    }
+    // inclusive scan: thread j ends with the map of the tiles of threads 0..j
+    for (int d = 1; d < kCarryThreads; d <<= 1) {
+      m0[j] = (unsigned char)f0;
+      m1[j] = (unsigned char)f1;
+      __syncthreads();
+      if (j >= d) {  // the earlier threads' map first, then this one's
+        const u32 e0 = m0[j - d], e1 = m1[j - d];
+        const u32 h0 = e0 ? f1 : f0, h1 = e1 ? f1 : f0;
+        f0 = h0;
+        f1 = h1;
+      }
+      __syncthreads();
+    }
+    m0[j] = (unsigned char)f0;
+    m1[j] = (unsigned char)f1;
+    __syncthreads();
+    const u32 cin = s_carry;
+    u32 c = j == 0 ? cin : (cin ? m1[j - 1] : m0[j - 1]);
+#pragma unroll 8
+    for (int i = 0; i < kCarryPer; ++i) {
+      const u32 v = sb[j * kCarryPer + i];
+      sb[j * kCarryPer + i] = (unsigned char)((v & 3) | (c << 2));
+      c = (v & 1) | ((v >> 1) & c);
+    }
+    __syncthreads();  // every thread has read s_carry and written its tiles
+    if (j == kCarryThreads - 1) s_carry = c;  // tiles past the range propagate: c is the carry out of c0 + n - 1
+#pragma unroll 8
+    for (int i = 0; i < kCarryPer; ++i) {
+      const u64 k = (u64)i * kCarryThreads + j;
+      if (k < n) flags[c0 + k] = sb[k];
+    }
+    __syncthreads();
+  }
+  if (j == 0) *chain = s_carry;
+}
+
+// Step 3: a tile whose carry-in is 1 adds it at its first limb; it ripples
+// while limbs wrap to zero, at most to the tile's end (a tile of all-ones
+// limbs passes the carry on through its propagate bit instead).
+__global__ void __launch_bounds__(256) carry_fix_kernel(const u32* flags, u64 t0, u64 t1, u64 total, u64* out,
+                                                        u64 out_limit, u64* side) {
+  const u64 t = t0 + (u64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= t1 || !((flags[t] >> 2) & 1)) return;
+  const u64 end = min((t + 1) * kScanTile, total);
+  for (u64 k = t * kScanTile; k < end; ++k) {
+    u64* q = k < out_limit ? out + k : side + (k - out_limit);
+    const u64 v = *q + 1;
+    *q = v;
+    if (v != 0) break;
+  }
 }
 
 // Adds side[0] + side[1]*B into out[0..L) and wraps the final carry around to
@@ -100,25 +204,40 @@ __global__ void wait_probe_kernel(const u32* flag, u32* err, int limit) {
   if (threadIdx.x == 0 && wait_flag(flag, limit) == 0) atomicExch(err, 1u);
 }
 
-// Tiles [tile_begin, tile_end) of the scan (all of them by default); the
-// status words are cleared with the first range, so the ranges of one scan
-// go in order on one stream.
+// Tiles [tile_begin, tile_end) of the scan (all of them by default).  The
+// ranges of one scan go in order on one stream (each range's carry-in comes
+// from the range before: through the status words of the lookback, or the
+// chain word of the three steps).
 template <class Prod>
 cudaError_t run_scan(const Prod& prod, u64 total, u64* out, u64 out_limit, Scan& sc, cudaStream_t st,
                      const char* name, u64 tile_begin = 0, u64 tile_end = ~0ull) {
   const u64 tiles = scan_tiles(total);
   tile_end = std::min(tile_end, tiles);
   cudaError_t e = scan_reserve(sc, tiles);
-  if (e != cudaSuccess) return e;
-  if (tile_begin == 0) {
-    e = cudaMemsetAsync(sc.flags, 0, (tiles + 1) * sizeof(u32), st);
+  if (e != cudaSuccess || tile_end <= tile_begin) return e;
+  const u64 n = tile_end - tile_begin;
+  if (tiles <= kLookbackTiles) {
+    if (tile_begin == 0) {
+      e = cudaMemsetAsync(sc.flags, 0, (tiles + 1) * sizeof(u32), st);
+      if (e != cudaSuccess) return e;
+    }
+    e = cudaMemsetAsync(sc.counter, 0, sizeof(u32), st);
     if (e != cudaSuccess) return e;
+    launch_begin(name, st);
+    scan_lookback_kernel<Prod><<<(unsigned)n, kScanThreads, 0, st>>>(prod, total, out, out_limit, sc.side, sc.flags,
+                                                                      sc.counter, sc.err, (u32)tile_begin);
+    launch_end(st);
+    return cudaGetLastError();
   }
-  e = cudaMemsetAsync(sc.counter, 0, sizeof(u32), st);
-  if (e != cudaSuccess) return e;
   launch_begin(name, st);
-  scan_kernel<Prod><<<(unsigned)(tile_end - tile_begin), kScanThreads, 0, st>>>(
-      prod, total, out, out_limit, sc.side, sc.flags, sc.counter, sc.err, (u32)tile_begin);
+  scan_kernel<Prod><<<(unsigned)n, kScanThreads, 0, st>>>(prod, total, out, out_limit, sc.side, sc.flags, tile_begin);
+  launch_end(st);
+  launch_begin("scan_tile_carries", st);
+  tile_carry_kernel<<<1, kCarryThreads, 0, st>>>(sc.flags, tile_begin, tile_end, sc.chain);
+  launch_end(st);
+  launch_begin("scan_carry_fix", st);
+  carry_fix_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(sc.flags, tile_begin, tile_end, total, out, out_limit,
+                                                                 sc.side);
   launch_end(st);
   return cudaGetLastError();
 }
@@ -143,6 +262,7 @@ cudaError_t scan_reserve(Scan& sc, u64 tiles) {
     e = cudaMalloc((void**)&sc.counter, 4 * sizeof(u32) + 4 * sizeof(u64));
     if (e != cudaSuccess) return e;
     sc.err = sc.counter + 1;
+    sc.chain = sc.counter + 2;
     sc.side = reinterpret_cast<u64*>(sc.counter + 4);
     e = cudaMemset(sc.counter, 0, 4 * sizeof(u32) + 4 * sizeof(u64));
   }

@@ -46,11 +46,12 @@ inline size_t tile_smem_bytes(int C, int R) {
   return C == 2 ? tile + (((size_t)1 << R) - 1) * 16 : tile;
 }
 
-// Scratch for the decoupled-lookback carry scan.
+// Scratch for the carry scan.
 struct Scan {
   u32* flags = nullptr;  // per-tile status words
   u32* counter = nullptr;
   u32* err = nullptr;    // nonzero after a lookback wait gave up
+  u32* chain = nullptr;  // carry between consecutive tile ranges of one scan
   u64* side = nullptr;   // limbs of the scan beyond the output (the carry words)
   u64 max_tiles = 0;
 };

@@ -12,17 +12,6 @@
 
 namespace nn {
 
-// Compile-time constants of p_i = c_i * 2^56 + 1 (ntt_info.h:69-73).
-template <int PR>
-struct PrimeC {
-  static constexpr u64 c = PR == 0 ? 27 : PR == 1 ? 58 : 87;
-  static constexpr u64 p = c << 56 | 1;
-  static constexpr u32 c_hi = (u32)(c << 24);
-  static constexpr u64 m64 = PR == 0 ? 10 : PR == 1 ? 5 : 3;  // ceil(2^64 / p)
-  // floor(2^(124+i) / p_i): the reference's Barrett constants (asmLinux.asm:926, 1075, 1236)
-  static constexpr u64 mu = PR == 0 ? 0x97b425ed097b4259ull : PR == 1 ? 0x8d3dcb08d3dcb08aull : 0xbc52640bc52640baull;
-};
-
 // Exact reduction of T < 2p^2 with the reference's Barrett constant and two
 // conditional subtractions (see barrett() in nn_device.cuh).
 template <int PR>
@@ -31,7 +20,7 @@ __device__ __forceinline__ u64 barrett_c(U128 t) {
   constexpr int sh = 60 + PR;
   const u64 top = (t.hi << (64 - sh)) | (t.lo >> sh);
   const u64 q = mulhi(top, PrimeC<PR>::mu);
-  u64 r = t.lo - mul_p(q, PrimeC<PR>::c_hi);
+  u64 r = t.lo + q * PrimeC<PR>::np;
   if (r >= p) r -= p;
   if (r >= p) r -= p;
   return r;
@@ -47,27 +36,31 @@ __device__ __forceinline__ u64 barrett_c(U128 t) {
 template <int PR>
 __device__ __forceinline__ void fwd_bfly_c(u64& x, u64& y, u64 w, u64 wp) {
   constexpr u64 p = PrimeC<PR>::p;
-  constexpr u32 ch = PrimeC<PR>::c_hi;
   if constexpr (PR < 2) {
-    const u64 r = y * w - mul_p(mulhi(y, wp), ch);  // signed, in [-p, p)
+    const u64 r = shoup_rem_c<PR>(y, w, wp);        // signed, in [-p, p)
     const u64 xr = x >= 2 * p ? x - 2 * p : x;      // [0, 2p)
     x = xr + r + p;                                 // [0, 4p)
     y = xr - r + p;                                 // [0, 4p)
-  } else {
-    fwd_bfly(x, y, w, wp, p, ch);
+  } else {  // asmLinux.asm:409-445: x, y in [0, 2p)
+    const u64 t = shoup_mul_c<PR>(y, w, wp);
+    const u64 xr = reduce2p(x, p);
+    x = xr + t;
+    y = xr + p - t;
   }
 }
 template <int PR>
 __device__ __forceinline__ void inv_bfly_c(u64& x, u64& y, u64 w, u64 wp) {
   constexpr u64 p = PrimeC<PR>::p;
-  constexpr u32 ch = PrimeC<PR>::c_hi;
   if constexpr (PR < 2) {
     const u64 d = x - y + 2 * p;                    // (0, 4p)
     const u64 sum = x + y;                          // [0, 4p)
     x = sum >= 2 * p ? sum - 2 * p : sum;           // [0, 2p)
-    y = d * w - mul_p(mulhi(d, wp), ch) + p;        // r in [-p, p) as a signed value; y in [0, 2p)
-  } else {
-    inv_bfly(x, y, w, wp, p, ch);
+    y = shoup_rem_c<PR>(d, w, wp) + p;              // r in [-p, p) as a signed value; y in [0, 2p)
+  } else {  // asmLinux.asm:595-630: x, y in [0, p)
+    const u64 s = reduce2p(x + y, p);
+    const u64 t = shoup_mul_c<PR>(x - y + p, w, wp);
+    x = s;
+    y = t;
   }
 }
 // Any lazy value of prime PR to [0, p).
@@ -315,8 +308,8 @@ __device__ __forceinline__ void pointwise4(u64 (&o)[4], const u64 (&A)[4], const
   constexpr u32 ch = PrimeC<PR>::c_hi;
   const u64 a0 = canon_c<PR>(A[0]), a1 = canon_c<PR>(A[1]), a2 = canon_c<PR>(A[2]), a3 = canon_c<PR>(A[3]);
   const u64 b0 = canon_c<PR>(Bv[0]), b1 = canon_c<PR>(Bv[1]), b2 = canon_c<PR>(Bv[2]), b3 = canon_c<PR>(Bv[3]);
-  const u64 wb1 = shoup_mul(b1, wv.x, wv.y, p, ch);
-  const u64 wb3 = shoup_mul(b3, wv.x, wv.y, p, ch);
+  const u64 wb1 = shoup_mul_c<PR>(b1, wv.x, wv.y);
+  const u64 wb3 = shoup_mul_c<PR>(b3, wv.x, wv.y);
   const u64 nwb3 = wb3 ? p - wb3 : 0;
   o[0] = barrett_c<PR>(add128(mul_wide(a0, b0), mul_wide(a1, wb1)));
   o[1] = barrett_c<PR>(add128(mul_wide(a0, b1), mul_wide(a1, b0)));

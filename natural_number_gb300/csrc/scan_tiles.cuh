@@ -60,15 +60,15 @@ struct CrtProducerT {
   }
   __device__ __forceinline__ W3 garner(u64 x0, u64 x1, u64 x2) const {
     const PrimeSet& P = g_primes;
-    const u64 p1 = P.p[1], p2 = P.p[2];
+    constexpr u64 p0 = PrimeC<0>::p, p1 = PrimeC<1>::p, p2 = PrimeC<2>::p;
     const u64 d1 = x1 >= x0 ? x1 - x0 : x1 + p1 - x0;
-    const u64 u = shoup_mul(d1, P.inv01, P.inv01s, p1, P.c_hi[1]);
+    const u64 u = shoup_mul_c<1>(d1, P.inv01, P.inv01s);
     const u64 d2 = x2 >= x0 ? x2 - x0 : x2 + p2 - x0;
-    const u64 t2 = shoup_mul(d2, P.inv02, P.inv02s, p2, P.c_hi[2]);
+    const u64 t2 = shoup_mul_c<2>(d2, P.inv02, P.inv02s);
     const u64 e2 = t2 >= u ? t2 - u : t2 + p2 - u;
-    const u64 v = shoup_mul(e2, P.inv12, P.inv12s, p2, P.c_hi[2]);
+    const u64 v = shoup_mul_c<2>(e2, P.inv12, P.inv12s);
     // lo = p0*u + x0
-    u64 l0 = P.p[0] * u, l1 = mulhi(P.p[0], u);
+    u64 l0 = p0 * u, l1 = mulhi(p0, u);
     l0 += x0;
     l1 += (l0 < x0);
     // m = p01_lo * v, h = p01_hi * v
@@ -244,8 +244,14 @@ __device__ __forceinline__ u32 wait_flag(const u32* f, int limit) {
 }
 
 // One tile of the scan over positions [0, total): limbs below out_limit go to
-// out, the rest to side.  Tiles of one scan must start in increasing order
+// out, the rest to side.
+// LOOKBACK: the tile takes its carry-in from its predecessors' status words
+// (decoupled lookback); tiles of one scan must then start in increasing order
 // (their predecessors already running), which the callers guarantee.
+// Without LOOKBACK the tile takes carry-in 0 and records in flags[tile] its
+// carry out for carry-in 0 (bit 0, generate) and whether a carry-in would pass
+// straight through (bit 1, propagate: every limb all ones); a later step
+// resolves the one-bit carries between tiles (carry.cu).
 // The scan's shared scratch: one block per kernel, whatever producers its
 // scan_tile instances take (a function's __shared__ variables exist once per
 // CTA, while each instance of a template would get its own).
@@ -260,7 +266,7 @@ __device__ __forceinline__ ScanShared& scan_shared() {
   return sh;
 }
 
-template <class Prod>
+template <class Prod, bool LOOKBACK = true>
 __device__ __forceinline__ void scan_tile(const Prod& prod, u64 tile, u64 total, u64* out, u64 out_limit, u64* side,
                                           u32* flags, u32* err) {
   constexpr int E = kScanE;
@@ -371,7 +377,9 @@ __device__ __forceinline__ void scan_tile(const Prod& prod, u64 tile, u64 total,
     }
     const u32 tg = c_if0, tp = c_if1 & !c_if0;
     u32 cin = 0;
-    if (tile > 0) {
+    if (!LOOKBACK) {
+      flags[tile] = tg | (tp << 1);
+    } else if (tile > 0) {
       flag_store(&flags[tile], kFlagAggregate | (tg << 2) | (tp << 3));
       long long j = (long long)tile - 1;
       for (;;) {
@@ -400,7 +408,7 @@ __device__ __forceinline__ void scan_tile(const Prod& prod, u64 tile, u64 total,
         --j;  // predecessor propagates: look further back
       }
     }
-    flag_store(&flags[tile], kFlagInclusive | ((tg | (tp & cin)) << 2));
+    if (LOOKBACK) flag_store(&flags[tile], kFlagInclusive | ((tg | (tp & cin)) << 2));
     s_cin = cin;
   }
   __syncthreads();

@@ -184,3 +184,33 @@ def test_large_unbalanced_products_mod_checks(ctx, na, nb):
     ma, mb, mp = mod_checks(a), mod_checks(b), mod_checks(prod)
     assert mp[0] == ma[0] * mb[0] % (2**64 - 1)
     assert mp[1] == ma[1] * mb[1] % (2**64 + 1)
+
+
+@pytest.mark.parametrize("n", [(1 << 21) + 3, 3 << 20])
+def test_carry_chains_across_many_scan_tiles(ctx, n):
+    """(B^n - 1)^2 = B^2n - 2 B^n + 1: its upper half is all-ones limbs, so
+    the CRT scan's tile carries propagate through thousands of tiles (scans
+    of more than 1024 tiles resolve them in separate steps rather than by the
+    lookback).  Through the device path and the host path, whose scan runs
+    in ranges of tiles with the copy-back of each range queued behind it."""
+    M = np.uint64(0xFFFFFFFFFFFFFFFF)
+    a = np.full(n, M, dtype=np.uint64)
+    want = np.concatenate([[np.uint64(1)], np.zeros(n - 1, dtype=np.uint64), [M - np.uint64(1)],
+                           np.full(n - 1, M, dtype=np.uint64)])
+    out = empty_dev(2 * n)
+    ctx.mul_device(out, to_dev(a), to_dev(a))
+    assert np.array_equal(to_host(out), want)
+    assert np.array_equal(ctx.mul(a, a), want)
+    assert np.array_equal(ctx.sqr(a), want)
+
+
+def test_multi_step_scan_vs_oracle(ctx, oracle):
+    """A 2^21 x 2^21-limb product (2048 scan tiles, past the lookback's 1024)
+    against the oracle, device and host paths."""
+    n = 1 << 21
+    a, b = limbs(61, n), limbs(62, n)
+    want = oracle.mul(a, b)
+    out = empty_dev(2 * n)
+    ctx.mul_device(out, to_dev(a), to_dev(b))
+    assert np.array_equal(to_host(out), want)
+    assert np.array_equal(ctx.mul(a, b), want)
