@@ -25,7 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["ntt.cu", "carry.cu", "batch.cu", "noalloc.cu"]
 CPP_SOURCES = ["engine.cpp", "profile.cpp", "natural_ops.cpp", "serve.cpp", "series.cpp", "host_glue.cpp", "divide.cpp",
                "host_pool.cpp"]
-HEADERS = ["nn_device.cuh", "nn_internal.h", "ntt_tiles.cuh", "scan_tiles.cuh", "context_access.h",
+HEADERS = ["nn_device.cuh", "nn_internal.h", "ntt_tiles.cuh", "scan_tiles.cuh", "tma.cuh", "context_access.h",
            "../../include/natural_gb300.hpp"]
 
 

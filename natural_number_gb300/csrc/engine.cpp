@@ -744,6 +744,7 @@ nn_status nn_context_create(int device, uint64_t budget, nn_context** out) {
     }
   }
   if (e == cudaSuccess) e = nn::scan_reserve(c->scan, 1024);
+  c->tables.err = c->scan.err;
   if (e != cudaSuccess) {
     nn_status st = e == cudaErrorNoDevice || e == cudaErrorNoKernelImageForDevice ? NN_ERR_NO_DEVICE : NN_ERR_CUDA;
     cudaGetLastError();

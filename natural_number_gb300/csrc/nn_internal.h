@@ -27,6 +27,7 @@ struct Tables {
   u64* iroot = nullptr;  // [3][cap] inverse
   u64 cap = 0;           // words per prime (= 2^(scale-1))
   int scale = 0;
+  u32* err = nullptr;    // device error word for kernels whose bounded waits run out (the context's)
 };
 cudaError_t tables_ensure(Tables& t, int s, cudaStream_t st);
 void tables_free(Tables& t);

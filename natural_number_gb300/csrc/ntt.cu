@@ -19,6 +19,7 @@
 // passes, staged in shared memory with the tile in the contiguous ones), and
 // writes the tile back.  The first forward pass reads limbs and reduces them on the fly; the
 // last inverse pass applies the 2^-(s-1) scale on the way out.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -26,6 +27,7 @@
 #include "nn_device.cuh"
 #include "nn_internal.h"
 #include "ntt_tiles.cuh"
+#include "tma.cuh"
 
 namespace nn {
 
@@ -130,8 +132,135 @@ __global__ void __launch_bounds__(256) pointwise_kernel(u64* dst, const u64* a, 
   pointwise_group<false>(dst, a, b, L, tab, tab_stride, blockIdx.y, g);
 }
 
+// Strided pass over residues with TMA: one CTA's tile (16 columns x 2^R
+// rows of one prime, R <= 9) is one or two boxes of the 3-D view
+// [3 * 2^lambda0 super-blocks][2^R rows][2^lg_s columns] of the residues,
+// loaded by one thread onto an mbarrier and stored back from shared memory
+// by the same engine.  The 16-column rows are 128 bytes, so the unpadded
+// tile has no bank conflicts (a warp reads two full rows).  SCALE applies
+// the 2^-(s-1) scale in shared memory before the store.
+template <bool INV, bool SCALE, int PR>
+__device__ __forceinline__ void col_tile_tma(u64* sm, u64* bar, const CUtensorMap* tm, int s, int lambda0, int R,
+                                             const u64* __restrict__ tw, u64 tile, u32* err) {
+  constexpr int C = 16;
+  constexpr u64 p = PrimeC<PR>::p;
+  const int lg_s = s - lambda0 - R;
+  const u64 tiles_per_sb = (1ull << lg_s) / C;
+  const u64 ksb = tile / tiles_per_sb;
+  const int x = (int)((tile % tiles_per_sb) * C);  // a multiple of 16 columns: 128-byte aligned
+  const int z = (int)(((u64)PR << lambda0) + ksb);
+  const u32 rows = 1u << R, nel = (u32)C << R, box_rows = rows < 256 ? rows : 256;
+  __shared__ int s_ok;
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    mbar_arrive_expect(bar, nel * 8);
+    for (u32 y = 0; y < rows; y += box_rows) tma_load_3d(sm + (u64)y * C, tm, x, (int)y, z, bar);
+    s_ok = mbar_wait(bar, 0);
+  }
+  __syncthreads();
+  if (!s_ok) {  // the copy never completed: record it, give the copy one more bounded wait, leave the tile
+    if (threadIdx.x == 0) {
+      if (err) atomicExch(err, 1u);
+      mbar_wait(bar, 0);
+    }
+    return;
+  }
+  mbar_wait(bar, 0);  // completed phase: this thread sees the copied tile
+  if (!INV)
+    tile_forward_any<C, PR, true, 3, false>(sm, R, ksb, tw, nullptr, 0);
+  else
+    tile_inverse_any<C, PR, true, 3, false>(sm, R, ksb, tw, nullptr, 0);
+  if (SCALE) {
+    for (u32 idx = 2 * threadIdx.x; idx < nel; idx += 2 * blockDim.x) {
+      ulonglong2 v = ld2<false>(sm + idx);
+      v.x = div_pow2(canon_c<PR>(v.x), (u32)(s - 1), p);
+      v.y = div_pow2(canon_c<PR>(v.y), (u32)(s - 1), p);
+      st2<false>(sm + idx, v);
+    }
+  }
+  fence_async_smem();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (u32 y = 0; y < rows; y += box_rows) tma_store_3d(tm, x, (int)y, z, sm + (u64)y * C);
+    bulk_store_drain();
+  }
+}
+
+template <bool INV, bool SCALE>
+__global__ void __launch_bounds__(256, 4) ntt_col_tma_kernel(const __grid_constant__ CUtensorMap tm, int s, int lambda0,
+                                                          int R, const u64* __restrict__ tab, u64 tab_stride,
+                                                          u32* err) {
+  extern __shared__ __align__(128) u64 sm[];
+  __shared__ __align__(8) u64 bar;
+  const u64* tw = tab + blockIdx.y * tab_stride;
+  if (blockIdx.y == 0)
+    col_tile_tma<INV, SCALE, 0>(sm, &bar, &tm, s, lambda0, R, tw, blockIdx.x, err);
+  else if (blockIdx.y == 1)
+    col_tile_tma<INV, SCALE, 1>(sm, &bar, &tm, s, lambda0, R, tw, blockIdx.x, err);
+  else
+    col_tile_tma<INV, SCALE, 2>(sm, &bar, &tm, s, lambda0, R, tw, blockIdx.x, err);
+}
+
+// cuTensorMapEncodeTiled from the driver, looked up once (nullptr where the
+// driver has none: the passes then keep their per-thread copies).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+  static const EncodeTiledFn fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      return (EncodeTiledFn) nullptr;
+    }
+    return reinterpret_cast<EncodeTiledFn>(f);
+  }();
+  return fn;
+}
+
+// The 3-D view of residues [3][2^s] for a strided pass over levels
+// [lambda0, lambda0 + R): 2^lg_s columns (contiguous), 2^R rows 2^lg_s words
+// apart, 3 * 2^lambda0 super-blocks of 2^(s - lambda0) words; boxes of 16
+// columns x min(2^R, 256) rows.
+bool col_tensor_map(CUtensorMap* m, const u64* res, int s, int lambda0, int R) {
+  const EncodeTiledFn enc = encode_tiled();
+  const int lg_s = s - lambda0 - R;
+  if (!enc || lg_s < 4 || R > 9 || (reinterpret_cast<uintptr_t>(res) & 15)) return false;
+  const cuuint64_t dims[3] = {1ull << lg_s, 1ull << R, 3ull << lambda0};
+  const cuuint64_t strides[2] = {8ull << lg_s, 8ull << (s - lambda0)};
+  const cuuint32_t box[3] = {16, (cuuint32_t)std::min(1 << R, 256), 1};
+  const cuuint32_t elem[3] = {1, 1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, const_cast<u64*>(res), dims, strides, box, elem,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <bool INV, bool SCALE>
+cudaError_t launch_col_tma(const CUtensorMap& tm, int s, const Pass& ps, const Tables& t, cudaStream_t st) {
+  const size_t smem = ((size_t)16 << ps.R) * 8;
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(ntt_col_tma_kernel<INV, SCALE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         200 * 1024);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  const u64 tiles = (1ull << s) / ((u64)16 << ps.R);
+  launch_begin(INV ? (SCALE ? "ntt_inv_last_col_pass" : "ntt_inv_col_pass") : "ntt_fwd_col_pass", st);
+  ntt_col_tma_kernel<INV, SCALE><<<dim3((unsigned)tiles, 3), 256, smem, st>>>(tm, s, ps.lambda0, ps.R,
+                                                                              INV ? t.iroot : t.root, t.cap, t.err);
+  launch_end(st);
+  return cudaGetLastError();
+}
+
 template <int C, bool FIRST, bool INV, bool SCALE>
 cudaError_t launch_pass(const u64* in, u64* out, u64 n_in, int s, const Pass& ps, const Tables& t, cudaStream_t st) {
+  if constexpr (C == 16 && !FIRST) {
+    CUtensorMap tm;
+    if (in == out && col_tensor_map(&tm, out, s, ps.lambda0, ps.R)) return launch_col_tma<INV, SCALE>(tm, s, ps, t, st);
+  }
   const size_t smem = tile_smem_bytes(ps.C, ps.R);
   static bool configured = false;
   if (!configured) {

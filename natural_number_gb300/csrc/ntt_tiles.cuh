@@ -124,14 +124,14 @@ __device__ __forceinline__ void stage_twiddles(u64* tws, const u64* tw, u64 ksb,
 // unit's rows are S = C * 2^nsub words apart, and the padded index is linear
 // in the row: pad16(x0 + m*S) = pad16(x0) + m*S + 2*floor(m*S/32) for every
 // unit of every tile shape used here, so each row is one add from the first.
-template <int K, int C, bool INV, int PR>
+template <int K, int C, bool INV, int PR, bool PAD = true>
 __device__ __forceinline__ void level_group(u64* sm, int l, int R, u64 ksb, const u64* __restrict__ tw,
                                             const u64* tws) {
   const int nsub = R - l - K;
   const u32 units = (u32)C << (R - K);
   const u32 tmask = (1u << nsub) - 1;
   const u32 S = (u32)C << nsub;
-  auto off = [S](u32 m) { return m * S + (((m * S) >> 5) << 1); };
+  auto off = [S](u32 m) { return PAD ? m * S + (((m * S) >> 5) << 1) : m * S; };
   const ulonglong2* twv = reinterpret_cast<const ulonglong2*>(tw);
   const ulonglong2* twsv = reinterpret_cast<const ulonglong2*>(tws);
   // twiddle pair g of local level l + lv for the unit of block rb
@@ -145,7 +145,7 @@ __device__ __forceinline__ void level_group(u64* sm, int l, int R, u64 ksb, cons
     const u32 rb = v >> nsub;
     const u32 row0 = (rb << (R - l)) + (v & tmask);
     const u64 bidx = (ksb << l) + rb;
-    u64* sp = sm + pad16(row0 * C + i);
+    u64* sp = sm + (PAD ? pad16(row0 * C + i) : row0 * C + i);
     u64 x[1 << K];
 #pragma unroll
     for (int m = 0; m < (1 << K); ++m) x[m] = sp[off(m)];
@@ -189,24 +189,24 @@ __device__ __forceinline__ int group_cap(int C, int R) {
   return k;
 }
 
-template <int C, bool INV, int PR>
+template <int C, bool INV, int PR, bool PAD = true>
 __device__ __forceinline__ void run_group(u64* sm, int k, int l, int R, u64 ksb, const u64* tw, const u64* tws) {
   if (k == 3)
-    level_group<3, C, INV, PR>(sm, l, R, ksb, tw, tws);
+    level_group<3, C, INV, PR, PAD>(sm, l, R, ksb, tw, tws);
   else if (k == 2)
-    level_group<2, C, INV, PR>(sm, l, R, ksb, tw, tws);
+    level_group<2, C, INV, PR, PAD>(sm, l, R, ksb, tw, tws);
   else
-    level_group<1, C, INV, PR>(sm, l, R, ksb, tw, tws);
+    level_group<1, C, INV, PR, PAD>(sm, l, R, ksb, tw, tws);
 }
 
 // Forward levels [l0, R) of the tile in shared memory.
-template <int C, int PR>
+template <int C, int PR, bool PAD = true>
 __device__ __forceinline__ void tile_forward(u64* sm, int R, u64 ksb, const u64* tw, const u64* tws, int l0 = 0) {
   const int cap = group_cap(C, R);
   const int n = (R - l0 + cap - 1) / cap;
   for (int g = 0, l = l0; g < n; ++g) {
     const int k = (R - l + (n - g) - 1) / (n - g);
-    run_group<C, false, PR>(sm, k, l, R, ksb, tw, tws);
+    run_group<C, false, PR, PAD>(sm, k, l, R, ksb, tw, tws);
     __syncthreads();
     l += k;
   }
@@ -223,47 +223,47 @@ __host__ __device__ constexpr int group_cap_ct(int C, int R, int maxk) {
   while (k > 1 && (C << (R - k)) < 256) --k;
   return k;
 }
-template <int C, int PR, int R, int L, int N, int G>
+template <int C, int PR, int R, int L, int N, int G, bool PAD = true>
 __device__ __forceinline__ void fwd_groups_ct(u64* sm, u64 ksb, const u64* tw, const u64* tws) {
   if constexpr (G < N) {
     constexpr int K = (R - L + (N - G) - 1) / (N - G);
-    level_group<K, C, false, PR>(sm, L, R, ksb, tw, tws);
+    level_group<K, C, false, PR, PAD>(sm, L, R, ksb, tw, tws);
     __syncthreads();
-    fwd_groups_ct<C, PR, R, L + K, N, G + 1>(sm, ksb, tw, tws);
+    fwd_groups_ct<C, PR, R, L + K, N, G + 1, PAD>(sm, ksb, tw, tws);
   }
 }
-template <int C, int PR, int R, int L0, int MAXK = 3>
+template <int C, int PR, int R, int L0, int MAXK = 3, bool PAD = true>
 __device__ __forceinline__ void tile_forward_ct(u64* sm, u64 ksb, const u64* tw, const u64* tws) {
   constexpr int cap = group_cap_ct(C, R, MAXK);
-  fwd_groups_ct<C, PR, R, L0, (R - L0 + cap - 1) / cap, 0>(sm, ksb, tw, tws);
+  fwd_groups_ct<C, PR, R, L0, (R - L0 + cap - 1) / cap, 0, PAD>(sm, ksb, tw, tws);
 }
 
 // Inverse levels R-1 .. l_stop of the tile in shared memory.
-template <int C, int PR>
+template <int C, int PR, bool PAD = true>
 __device__ __forceinline__ void tile_inverse(u64* sm, int R, u64 ksb, const u64* tw, const u64* tws, int l_stop = 0) {
   const int cap = group_cap(C, R);
   const int n = (R - l_stop + cap - 1) / cap;
   for (int g = 0, l = R; g < n; ++g) {
     const int k = (l - l_stop + (n - g) - 1) / (n - g);
     l -= k;
-    run_group<C, true, PR>(sm, k, l, R, ksb, tw, tws);
+    run_group<C, true, PR, PAD>(sm, k, l, R, ksb, tw, tws);
     __syncthreads();
   }
 }
 // Inverse groups from level L (exclusive) down to LSTOP.
-template <int C, int PR, int R, int L, int LSTOP, int N, int G>
+template <int C, int PR, int R, int L, int LSTOP, int N, int G, bool PAD = true>
 __device__ __forceinline__ void inv_groups_ct(u64* sm, u64 ksb, const u64* tw, const u64* tws) {
   if constexpr (G < N) {
     constexpr int K = (L - LSTOP + (N - G) - 1) / (N - G);
-    level_group<K, C, true, PR>(sm, L - K, R, ksb, tw, tws);
+    level_group<K, C, true, PR, PAD>(sm, L - K, R, ksb, tw, tws);
     __syncthreads();
-    inv_groups_ct<C, PR, R, L - K, LSTOP, N, G + 1>(sm, ksb, tw, tws);
+    inv_groups_ct<C, PR, R, L - K, LSTOP, N, G + 1, PAD>(sm, ksb, tw, tws);
   }
 }
-template <int C, int PR, int R, int LSTOP, int MAXK = 3>
+template <int C, int PR, int R, int LSTOP, int MAXK = 3, bool PAD = true>
 __device__ __forceinline__ void tile_inverse_ct(u64* sm, u64 ksb, const u64* tw, const u64* tws) {
   constexpr int cap = group_cap_ct(C, R, MAXK);
-  inv_groups_ct<C, PR, R, R, LSTOP, (R - LSTOP + cap - 1) / cap, 0>(sm, ksb, tw, tws);
+  inv_groups_ct<C, PR, R, R, LSTOP, (R - LSTOP + cap - 1) / cap, 0, PAD>(sm, ksb, tw, tws);
 }
 
 // Forward levels [l0, R) / inverse levels R-1 .. l_stop: the compile-time
@@ -271,32 +271,32 @@ __device__ __forceinline__ void tile_inverse_ct(u64* sm, u64 ksb, const u64* tw,
 // passes of 7-9 levels, contiguous passes of 10-11), the runtime loop
 // otherwise.  Only the per-call kernels take them (CT); the batch kernel
 // keeps one code path per width.
-template <int C, int PR, bool CT, int MAXK = 3>
+template <int C, int PR, bool CT, int MAXK = 3, bool PAD = true>
 __device__ __forceinline__ void tile_forward_any(u64* sm, int R, u64 ksb, const u64* tw, const u64* tws, int l0) {
   if constexpr (CT && C == 2) {
-    if (R == 11 && l0 == 0) return tile_forward_ct<C, PR, 11, 0, MAXK>(sm, ksb, tw, tws);
-    if (R == 10 && l0 == 0) return tile_forward_ct<C, PR, 10, 0>(sm, ksb, tw, tws);
+    if (R == 11 && l0 == 0) return tile_forward_ct<C, PR, 11, 0, MAXK, PAD>(sm, ksb, tw, tws);
+    if (R == 10 && l0 == 0) return tile_forward_ct<C, PR, 10, 0, 3, PAD>(sm, ksb, tw, tws);
   } else if constexpr (CT && C == 16) {
-    if (R == 8 && l0 == 0) return tile_forward_ct<C, PR, 8, 0>(sm, ksb, tw, tws);
-    if (R == 8 && l0 == 1) return tile_forward_ct<C, PR, 8, 1>(sm, ksb, tw, tws);
-    if (R == 9 && l0 == 0) return tile_forward_ct<C, PR, 9, 0>(sm, ksb, tw, tws);
-    if (R == 9 && l0 == 1) return tile_forward_ct<C, PR, 9, 1>(sm, ksb, tw, tws);
-    if (R == 7 && l0 == 0) return tile_forward_ct<C, PR, 7, 0>(sm, ksb, tw, tws);
-    if (R == 7 && l0 == 1) return tile_forward_ct<C, PR, 7, 1>(sm, ksb, tw, tws);
+    if (R == 8 && l0 == 0) return tile_forward_ct<C, PR, 8, 0, 3, PAD>(sm, ksb, tw, tws);
+    if (R == 8 && l0 == 1) return tile_forward_ct<C, PR, 8, 1, 3, PAD>(sm, ksb, tw, tws);
+    if (R == 9 && l0 == 0) return tile_forward_ct<C, PR, 9, 0, 3, PAD>(sm, ksb, tw, tws);
+    if (R == 9 && l0 == 1) return tile_forward_ct<C, PR, 9, 1, 3, PAD>(sm, ksb, tw, tws);
+    if (R == 7 && l0 == 0) return tile_forward_ct<C, PR, 7, 0, 3, PAD>(sm, ksb, tw, tws);
+    if (R == 7 && l0 == 1) return tile_forward_ct<C, PR, 7, 1, 3, PAD>(sm, ksb, tw, tws);
   }
-  tile_forward<C, PR>(sm, R, ksb, tw, tws, l0);
+  tile_forward<C, PR, PAD>(sm, R, ksb, tw, tws, l0);
 }
-template <int C, int PR, bool CT, int MAXK = 3>
+template <int C, int PR, bool CT, int MAXK = 3, bool PAD = true>
 __device__ __forceinline__ void tile_inverse_any(u64* sm, int R, u64 ksb, const u64* tw, const u64* tws, int l_stop) {
   if constexpr (CT && C == 2) {
-    if (R == 11 && l_stop == 0) return tile_inverse_ct<C, PR, 11, 0, MAXK>(sm, ksb, tw, tws);
-    if (R == 10 && l_stop == 0) return tile_inverse_ct<C, PR, 10, 0>(sm, ksb, tw, tws);
+    if (R == 11 && l_stop == 0) return tile_inverse_ct<C, PR, 11, 0, MAXK, PAD>(sm, ksb, tw, tws);
+    if (R == 10 && l_stop == 0) return tile_inverse_ct<C, PR, 10, 0, 3, PAD>(sm, ksb, tw, tws);
   } else if constexpr (CT && C == 16) {
-    if (R == 8 && l_stop == 0) return tile_inverse_ct<C, PR, 8, 0>(sm, ksb, tw, tws);
-    if (R == 9 && l_stop == 0) return tile_inverse_ct<C, PR, 9, 0>(sm, ksb, tw, tws);
-    if (R == 7 && l_stop == 0) return tile_inverse_ct<C, PR, 7, 0>(sm, ksb, tw, tws);
+    if (R == 8 && l_stop == 0) return tile_inverse_ct<C, PR, 8, 0, 3, PAD>(sm, ksb, tw, tws);
+    if (R == 9 && l_stop == 0) return tile_inverse_ct<C, PR, 9, 0, 3, PAD>(sm, ksb, tw, tws);
+    if (R == 7 && l_stop == 0) return tile_inverse_ct<C, PR, 7, 0, 3, PAD>(sm, ksb, tw, tws);
   }
-  tile_inverse<C, PR>(sm, R, ksb, tw, tws, l_stop);
+  tile_inverse<C, PR, PAD>(sm, R, ksb, tw, tws, l_stop);
 }
 
 // Pointwise product of one group of 4 residues (a0..a3)(b0..b3), lazy forward
