@@ -201,6 +201,147 @@ __global__ void __launch_bounds__(256, 4) ntt_col_tma_kernel(const __grid_consta
     col_tile_tma<INV, SCALE, 2>(sm, &bar, &tm, s, lambda0, R, tw, blockIdx.x, err);
 }
 
+// All threads learn whether the copies of phase `parity` completed: thread 0
+// waits (bounded), the others then observe the completed phase, which makes
+// the copied bytes visible to them.  A wait that ran out is recorded in *err;
+// thread 0 gives the copies one more bounded wait before the tile is left.
+__device__ __forceinline__ bool tile_arrived(u64* bar, u32 parity, u32* err, int* s_ok) {
+  if (threadIdx.x == 0) *s_ok = mbar_wait(bar, parity);
+  __syncthreads();
+  if (!*s_ok) {
+    if (threadIdx.x == 0) {
+      if (err) atomicExch(err, 1u);
+      mbar_wait(bar, parity);
+    }
+    return false;
+  }
+  mbar_wait(bar, parity);
+  return true;
+}
+
+// Groups of 4 residues a thread takes in the fused bulk pass's pointwise
+// product (256 threads): 4 for tiles of 2^11 rows (4096 residues, three CTAs
+// an SM), 2 for tiles of up to 2^10 rows (four CTAs an SM, 64 registers).
+constexpr int kPointwiseGroups = 4;
+
+// Contiguous pass with bulk copies: a tile is 2 columns x 2^R rows of one
+// prime, 2^(R+1) consecutive residues, which arrive as 256-byte runs placed
+// at the padded layout's 34-word stride (pad16 of word 32c is 34c), while
+// the tile's 2^R - 1 twiddle pairs arrive as one run per level (level j:
+// 2^j pairs from ksb * 2^j); all complete on one mbarrier.  FUSED (256
+// threads, at most 4 * PG * 256 residues): after the forward levels each
+// thread keeps the twiddle pairs and the other operand's residues of its PG
+// pointwise groups in registers, so the inverse twiddle pairs (the barrier's
+// second phase) are copied into the same shared words while the pointwise
+// product (by `other`; nullptr squares) runs; then the inverse levels.  The
+// tile goes back as 256-byte runs.
+template <bool INV, bool FUSED, int PR, int MAXK, int PG = kPointwiseGroups>
+__device__ __forceinline__ void row_tile_bulk(u64* sm, u64* bar, u64* res, const u64* other, int s, int R,
+                                              const u64* __restrict__ tab, const u64* __restrict__ itab,
+                                              u64 tab_stride, u64 tile, u32* err) {
+  constexpr int C = 2;
+  const u32 nel = (u32)C << R;
+  const u64 ksb = tile;  // a contiguous pass has one tile per block of 2^(R+1) words
+  u64* g = res + ((u64)PR << s) + (ksb << (R + 1));
+  const u32 run = nel < 32 ? nel : 32;
+  const u32 nruns = nel / run;
+  const u64* tw = tab + (u64)PR * tab_stride;
+  u64* tws = sm + tile_words(nel);
+  __shared__ int s_ok;
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    mbar_arrive_expect(bar, nel * 8 + 16u * ((1u << R) - 1));
+  }
+  __syncthreads();
+  for (u32 c = threadIdx.x; c < nruns; c += blockDim.x) bulk_load(sm + 34 * c, g + (u64)run * c, run * 8, bar);
+  for (int j = threadIdx.x; j < R; j += blockDim.x)
+    bulk_load(tws + 2 * ((1u << j) - 1), tw + 2 * (ksb << j), 16u << j, bar);
+  if (!tile_arrived(bar, 0, err, &s_ok)) return;
+  if (!INV) {
+    tile_forward_any<C, PR, true, MAXK>(sm, R, ksb, tw, tws, 0);
+    if (FUSED) {
+      const ulonglong2* twsv = reinterpret_cast<const ulonglong2*>(tws);
+      const u64* oth = other ? other + ((u64)PR << s) + (ksb << (R + 1)) : nullptr;
+      const u32 deep = (1u << (R - 1)) - 1;  // local level R-1: the blocks of 4 residues
+      ulonglong2 pw[PG], A01[PG], A23[PG];
+#pragma unroll
+      for (int k = 0; k < PG; ++k) {
+        const u32 g4 = 4 * (threadIdx.x + k * blockDim.x);
+        if (g4 < nel) {
+          pw[k] = twsv[deep + (g4 >> 2)];
+          if (oth) {
+            A01[k] = ld2<false>(oth + g4);
+            A23[k] = ld2<false>(oth + g4 + 2);
+          }
+        }
+      }
+      fence_async_smem();  // the forward pairs have been read before the inverse ones overwrite them
+      __syncthreads();
+      if (threadIdx.x == 0) mbar_arrive_expect(bar, 16u * ((1u << R) - 1));
+      const u64* itw = itab + (u64)PR * tab_stride;
+      for (int j = threadIdx.x; j < R; j += blockDim.x)
+        bulk_load(tws + 2 * ((1u << j) - 1), itw + 2 * (ksb << j), 16u << j, bar);
+#pragma unroll
+      for (int k = 0; k < PG; ++k) {
+        const u32 g4 = 4 * (threadIdx.x + k * blockDim.x);
+        if (g4 < nel) {
+          const u64 Bv[4] = {sm[pad16(g4)], sm[pad16(g4 + 1)], sm[pad16(g4 + 2)], sm[pad16(g4 + 3)]};
+          const u64 A[4] = {oth ? A01[k].x : Bv[0], oth ? A01[k].y : Bv[1], oth ? A23[k].x : Bv[2],
+                            oth ? A23[k].y : Bv[3]};
+          u64 o[4];
+          pointwise4<PR>(o, A, Bv, pw[k]);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) sm[pad16(g4 + q)] = o[q];
+        }
+      }
+      if (!tile_arrived(bar, 1, err, &s_ok)) return;  // its barrier also orders the products before the levels
+      tile_inverse_any<C, PR, true, MAXK>(sm, R, ksb, itw, tws, 0);
+    }
+  } else {
+    tile_inverse_any<C, PR, true>(sm, R, ksb, tw, tws, 0);
+  }
+  fence_async_smem();
+  __syncthreads();
+  for (u32 c = threadIdx.x; c < nruns; c += blockDim.x) bulk_store(g + (u64)run * c, sm + 34 * c, run * 8);
+  if (threadIdx.x < nruns) bulk_store_drain();
+}
+
+template <bool INV>
+__global__ void __launch_bounds__(256, 4) ntt_row_bulk_kernel(u64* res, int s, int R, const u64* __restrict__ tab,
+                                                           u64 tab_stride, u32* err) {
+  extern __shared__ __align__(128) u64 sm[];
+  __shared__ __align__(8) u64 bar;
+  if (blockIdx.y == 0)
+    row_tile_bulk<INV, false, 0, 3>(sm, &bar, res, nullptr, s, R, tab, nullptr, tab_stride, blockIdx.x, err);
+  else if (blockIdx.y == 1)
+    row_tile_bulk<INV, false, 1, 3>(sm, &bar, res, nullptr, s, R, tab, nullptr, tab_stride, blockIdx.x, err);
+  else
+    row_tile_bulk<INV, false, 2, 3>(sm, &bar, res, nullptr, s, R, tab, nullptr, tab_stride, blockIdx.x, err);
+}
+
+// The fused last pass with bulk copies; register budgets as ntt_fused_kernel.
+template <int BLOCKS>
+__global__ void __launch_bounds__(256, BLOCKS) ntt_fused_bulk_kernel(u64* res, const u64* other, int s, int R,
+                                                                  const u64* __restrict__ tab,
+                                                                  const u64* __restrict__ itab, u64 tab_stride,
+                                                                  u32* err) {
+  extern __shared__ __align__(128) u64 sm[];
+  __shared__ __align__(8) u64 bar;
+  constexpr int K = BLOCKS == 3 ? 4 : 3;
+  constexpr int PG = BLOCKS == 3 ? kPointwiseGroups : kPointwiseGroups / 2;
+  if (blockIdx.y == 0)
+    row_tile_bulk<false, true, 0, K, PG>(sm, &bar, res, other, s, R, tab, itab, tab_stride, blockIdx.x, err);
+  else if (blockIdx.y == 1)
+    row_tile_bulk<false, true, 1, K, PG>(sm, &bar, res, other, s, R, tab, itab, tab_stride, blockIdx.x, err);
+  else
+    row_tile_bulk<false, true, 2, K, PG>(sm, &bar, res, other, s, R, tab, itab, tab_stride, blockIdx.x, err);
+}
+
+// Bulk copies want 16-byte aligned global runs: the residue arrays of the
+// context's buffers always are; an unaligned caller buffer keeps the
+// per-thread copies.
+inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
 // cuTensorMapEncodeTiled from the driver, looked up once (nullptr where the
 // driver has none: the passes then keep their per-thread copies).
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -260,6 +401,24 @@ cudaError_t launch_pass(const u64* in, u64* out, u64 n_in, int s, const Pass& ps
   if constexpr (C == 16 && !FIRST) {
     CUtensorMap tm;
     if (in == out && col_tensor_map(&tm, out, s, ps.lambda0, ps.R)) return launch_col_tma<INV, SCALE>(tm, s, ps, t, st);
+  }
+  if constexpr (C == 2 && !FIRST && !SCALE) {
+    if (in == out && aligned16(out) && ps.lambda0 + ps.R == s - 1) {
+      const size_t smem = tile_smem_bytes(2, ps.R);
+      static bool configured = false;
+      if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(ntt_row_bulk_kernel<INV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             200 * 1024);
+        if (e != cudaSuccess) return e;
+        configured = true;
+      }
+      const u64 tiles = (1ull << s) / ((u64)2 << ps.R);
+      launch_begin(INV ? "ntt_inv_row_pass" : "ntt_fwd_row_pass", st);
+      ntt_row_bulk_kernel<INV><<<dim3((unsigned)tiles, 3), 256, smem, st>>>(out, s, ps.R, INV ? t.iroot : t.root,
+                                                                             t.cap, t.err);
+      launch_end(st);
+      return cudaGetLastError();
+    }
   }
   const size_t smem = tile_smem_bytes(ps.C, ps.R);
   static bool configured = false;
@@ -419,6 +578,26 @@ cudaError_t ntt_fused_last(u64* res, const u64* other, int s, const Tables& t, c
   }
   const u64 tiles = (1ull << s) / ((u64)ps.C << ps.R);
   dim3 grid((unsigned)tiles, 3);
+  const u64 nel = (u64)2 << ps.R;
+  if (aligned16(res) && (!other || aligned16(other)) && ps.lambda0 + ps.R == s - 1 &&
+      nel <= (u64)4 * kPointwiseGroups * 256) {
+    static bool bulk_configured = false;
+    if (!bulk_configured) {
+      cudaError_t e = cudaFuncSetAttribute(ntt_fused_bulk_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           200 * 1024);
+      if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(ntt_fused_bulk_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      if (e != cudaSuccess) return e;
+      bulk_configured = true;
+    }
+    launch_begin("ntt_fused_row_pass", st);
+    if (4 * smem <= 227 * 1024 && nel <= (u64)2 * kPointwiseGroups * 256)
+      ntt_fused_bulk_kernel<4><<<grid, 256, smem, st>>>(res, other, s, ps.R, t.root, t.iroot, t.cap, t.err);
+    else
+      ntt_fused_bulk_kernel<3><<<grid, 256, smem, st>>>(res, other, s, ps.R, t.root, t.iroot, t.cap, t.err);
+    launch_end(st);
+    return cudaGetLastError();
+  }
   launch_begin("ntt_fused_row_pass", st);
   if (4 * smem <= 227 * 1024)
     ntt_fused_kernel<4><<<grid, 256, smem, st>>>(res, other, s, ps.lambda0, ps.R, t.root, t.iroot, t.cap);
