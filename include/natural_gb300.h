@@ -294,9 +294,11 @@ nn_status nn_e_dec_host(nn_context* ctx, uint64_t terms, uint64_t digits, char**
 
 /* The same recipes with the binary-splitting trees and the decimal split tree
  * evaluated level by level, each level's products as one GPU batch; the
- * bottom subtrees, whose values stay below about host_below limbs (256 is a
- * good choice; host_below / 2 for the decimal split), run whole on host
- * threads.
+ * series trees' bottom subtrees, whose values stay below about host_below
+ * limbs (256 is a good choice), run whole on host threads.  The decimal split
+ * runs its levels while the split powers have at least host_below / 2 limbs;
+ * the nodes left become digits on the device (one thread a node peels off
+ * 18-digit groups, natural.h:566-573 and 994-1011) and come back in one copy.
  * terms must be a power of two (the trees are then perfect).  timing (8
  * doubles, may be NULL): total s, tree s, division s, decimal s, GPU-batch s,
  * host-product s, GPU products, host products. */

@@ -22,7 +22,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = shutil.which("nvcc") or os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["ntt.cu", "carry.cu", "batch.cu", "noalloc.cu"]
+CU_SOURCES = ["ntt.cu", "carry.cu", "batch.cu", "noalloc.cu", "decimal.cu"]
 CPP_SOURCES = ["engine.cpp", "profile.cpp", "natural_ops.cpp", "serve.cpp", "series.cpp", "host_glue.cpp", "divide.cpp",
                "host_pool.cpp"]
 HEADERS = ["nn_device.cuh", "nn_internal.h", "ntt_tiles.cuh", "scan_tiles.cuh", "tma.cuh", "context_access.h",

@@ -33,10 +33,12 @@
 
 #include "../../include/natural_gb300.h"
 #include "../../include/natural_gb300.hpp"
+#include "nn_internal.h"
 
 namespace {
 
 using u64 = uint64_t;
+using u32 = uint32_t;
 using u128 = unsigned __int128;
 using Clock = std::chrono::steady_clock;
 
@@ -181,20 +183,6 @@ u64 sub_span(u64* out, const u64* a, u64 na, const u64* b, u64 nb) {
 // |a - b| as natural::operator- computes it (natural.h:324-343); out may be a or b.
 u64 absdiff_span(u64* out, const u64* a, u64 na, const u64* b, u64 nb) {
   return cmp_span(a, na, b, nb) >= 0 ? sub_span(out, a, na, b, nb) : sub_span(out, b, nb, a, na);
-}
-
-// out = a >> bits; out may be a.
-u64 shr_span(u64* out, const u64* a, u64 na, u64 bits) {
-  const u64 w = bits >> 6, s = bits & 63;
-  if (w >= na) return 0;
-  const u64 n = na - w;
-  if (s == 0) {
-    std::memmove(out, a + w, 8 * n);
-  } else {
-    for (u64 i = 0; i + 1 < n; ++i) out[i] = (a[w + i] >> s) | (a[w + i + 1] << (64 - s));
-    out[n - 1] = a[w + n - 1] >> s;
-  }
-  return norm(out, n);
 }
 
 natural to_natural(const u64* a, u64 n) {
@@ -569,66 +557,25 @@ struct DecLevel {  // base[i] = 10^(18 * 2^i), its reciprocal and shift, as span
   u64 shift;  // ((base.size + 2) << 6) - n_shl
 };
 
-// The split by 10^18 of v < 10^36 (i == 0, natural.h:954-955) and the two
-// 18-digit leaves; the first node omits leading zeros.
-u64 dec_leaf(const u64* v, u64 nv, bool first, char* out) {
-  const u128 x = nv == 0 ? 0 : nv == 1 ? (u128)v[0] : ((u128)v[1] << 64 | v[0]);
-  const u64 q = (u64)(x / nn_gb300::dec_base_0), r = (u64)(x % nn_gb300::dec_base_0);
-  char buf[48];
-  int n;
-  if (first && q == 0)
-    n = std::snprintf(buf, sizeof buf, "%llu", (unsigned long long)r);
-  else if (first)
-    n = std::snprintf(buf, sizeof buf, "%llu%018llu", (unsigned long long)q, (unsigned long long)r);
-  else
-    n = std::snprintf(buf, sizeof buf, "%018llu%018llu", (unsigned long long)q, (unsigned long long)r);
-  std::memcpy(out, buf, n);
-  return (u64)n;
-}
-
-// Scratch words for dec_subtree at level i.
-u64 dec_scratch(const std::vector<DecLevel>& D, int i) {
-  u64 w = 64;
-  for (int k = 1; k <= i; ++k) w += D[k].nr + 5 * D[k].nb + 32;
-  return w;
-}
-
-// Digits of v (v < base[i]^2) split at level i (0: the leaf split) into out;
-// a node that is not first writes exactly 18 * 2^(i+1) digits.  Returns the
-// number of digits written.
-u64 dec_subtree(const std::vector<DecLevel>& D, const u64* v, u64 nv, int i, bool first, char* out, u64* tmp) {
-  if (i == 0) return dec_leaf(v, nv, first, out);
-  const DecLevel& L = D[i];
-  // hi = base_r * (v >> ((base.size - 1) << 6)) >> shift   (natural.h:958-960)
-  const u64 ny = nv > L.nb - 1 ? nv - (L.nb - 1) : 0;
-  u64* hi = tmp;  // nr + nb + 4 words
-  u64 nh = mul_span(hi, L.base_r, L.nr, v + (L.nb - 1), ny);
-  nh = shr_span(hi, hi, nh, L.shift);
-  // lo = |v - base * hi|, then the correction loop (natural.h:961-966)
-  u64* p = hi + L.nr + L.nb + 4;  // 2 nb + 8 words
-  const u64 np = mul_span(p, L.base, L.nb, hi, nh);
-  u64* lo = p + 2 * L.nb + 8;  // 2 nb + 8 words
-  u64 nl = absdiff_span(lo, v, nv, p, np);
-  while (cmp_span(lo, nl, L.base, L.nb) >= 0) {
-    const u64 one[1] = {1};
-    hi[nh] = 0;
-    nh = add_span(hi, hi, nh, one, 1);
-    nl = sub_span(lo, lo, nl, L.base, L.nb);
+char* export_str(const std::string& s, u64* n) {
+  *n = s.size();
+  char* p = (char*)std::malloc(s.size() + 1);
+  if (p) {
+    std::memcpy(p, s.data(), s.size());
+    p[s.size()] = 0;
   }
-  u64* rest = lo + 2 * L.nb + 8;
-  if (first && nh == 0) return dec_subtree(D, lo, nl, i - 1, true, out, rest);
-  const u64 w = dec_subtree(D, hi, nh, i - 1, first, out, rest);
-  return w + dec_subtree(D, lo, nl, i - 1, false, out + w, rest);
+  return p;
 }
 
-// Decimal digits (std::formatter<natural>, natural.h:1089-1091): the split
-// tree of _format_dec, level by level with GPU batches while the split
-// powers are at least host_below / 2 limbs, then whole subtrees on host
-// threads.
-std::string to_dec_levels(nn_context* c, const natural& x, u64 host_below, Staging& stg, Stats& S) {
+// Decimal digits (std::formatter<natural>, natural.h:1089-1091) into a
+// malloc'd, NUL-terminated buffer of *len digits: the split tree of
+// _format_dec, level by level with GPU batches while the split powers are at
+// least host_below / 2 limbs; the nodes left are turned into digits on the
+// device, one thread a node (decimal.cu), and come back in one copy.
+char* to_dec_levels(nn_context* c, const natural& x, u64 host_below, Staging& stg, Stats& S, u64* len) {
   using namespace nn_gb300;
   const int top = dec_init(x);
-  if (top < 0) return std::to_string(x[0]);
+  if (top < 0) return export_str(std::to_string(x[0]), len);
   DecCache& C = dec_cache();
   std::vector<DecLevel> D(top + 1);
   for (int i = 1; i <= top; ++i) {
@@ -689,36 +636,59 @@ std::string to_dec_levels(nn_context* c, const natural& x, u64 host_below, Stagi
     }
     lv.swap(next);
   }
-  // The rest on host threads: node 0 (the first) may be shorter, every other
-  // node writes exactly 18 * 2^(i+1) digits.
+  // The nodes left, each below base[i]^2 = 10^(18 * 2^(i+1)), on the device:
+  // limb-major in one upload, 2^(i+1) groups of 18 digits a node written in
+  // place of the tree's leaves (natural.h:994-1011); node 0, the first, is
+  // written at the same width and loses its leading zeros on the way back.
   const auto t0 = Clock::now();
-  const u64 width = 18ull << (i + 1);
-  const u64 scratch = dec_scratch(D, i);
-  std::string head(width + 64, '\0');
-  {
-    const natural& v0 = lv[0].v;
-    head.resize(dec_subtree(D, v0.data, span_len(v0), i, lv[0].first, head.data(), scratch_words(scratch)));
-  }
-  std::string out(head.size() + (lv.size() - 1) * width, '\0');
-  std::memcpy(out.data(), head.data(), head.size());
-  char* body = out.data() + head.size();
-  parallel_for(lv.size() - 1, 1, [&](u64 k) {
-    const natural& v = lv[k + 1].v;
-    dec_subtree(D, v.data, span_len(v), i, false, body + k * width, scratch_words(scratch));
+  const u64 n = lv.size();
+  const u32 groups = 2u << i;
+  const u64 width = 18ull * groups;
+  u64 maxlen = 0;
+  for (const Node& nd : lv) maxlen = std::max(maxlen, span_len(nd.v));
+  const u64 words = maxlen * n + (n + 1) / 2;  // limbs, then the u32 lengths
+  u64* hw = stg.in.get(words);
+  u32* hlen = reinterpret_cast<u32*>(hw + maxlen * n);
+  constexpr u64 kBlock = 64;  // nodes a task transposes: 512-byte runs of each limb row
+  parallel_for((n + kBlock - 1) / kBlock, 1, [&](u64 blk) {
+    const u64 k0 = blk * kBlock, k1 = std::min(n, k0 + kBlock);
+    for (u64 k = k0; k < k1; ++k) hlen[k] = (u32)span_len(lv[k].v);
+    for (u64 j = 0; j < maxlen; ++j)
+      for (u64 k = k0; k < k1; ++k) hw[j * n + k] = j < hlen[k] ? lv[k].v.data[j] : 0;
   });
-  S.host_s += since(t0);
+  cudaStream_t st = (cudaStream_t)nn_context_stream(c);
+  u64* dw = nullptr;
+  char* dout = nullptr;
+  check_cuda(cudaMallocAsync((void**)&dw, 8 * words, st), "decimal nodes");
+  check_cuda(cudaMallocAsync((void**)&dout, n * width, st), "decimal digits");
+  check_cuda(cudaMemcpyAsync(dw, hw, 8 * words, cudaMemcpyHostToDevice, st), "upload");
+  check_cuda(nn::dec_groups(dw, reinterpret_cast<const u32*>(dw + maxlen * n), n, groups, dout, st), "decimal kernel");
+  std::string head(width, '0');
+  check_cuda(cudaMemcpyAsync(head.data(), dout, width, cudaMemcpyDeviceToHost, st), "download");
+  check_cuda(cudaStreamSynchronize(st), "decimal digits");
+  u64 off = 0;
+  while (off + 1 < width && head[off] == '0') ++off;
+  const u64 total = n * width - off;
+  char* out = static_cast<char*>(std::malloc(total + 1));
+  if (!out) {
+    cudaFreeAsync(dw, st);
+    cudaFreeAsync(dout, st);
+    throw std::bad_alloc();
+  }
+  cudaError_t e = cudaMemcpyAsync(out, dout + off, total, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFreeAsync(dw, st);
+  cudaFreeAsync(dout, st);
+  if (e != cudaSuccess) {
+    std::free(out);
+    check_cuda(e, "download");
+  }
+  out[total] = 0;
+  *len = total;
+  S.gpu_s += since(t0);
   return out;
 }
 
-char* export_str(const std::string& s, u64* n) {
-  *n = s.size();
-  char* p = (char*)std::malloc(s.size() + 1);
-  if (p) {
-    std::memcpy(p, s.data(), s.size());
-    p[s.size()] = 0;
-  }
-  return p;
-}
 
 void fill_timing(double* t, const double* v, int k) {
   if (t)
@@ -746,12 +716,12 @@ nn_status nn_pi_dec_levels(nn_context* c, uint64_t terms, uint64_t acc, uint64_t
     num *= denc;
     den /= num;
     const double t_div = since(t0) - t_tree;
-    std::string s = to_dec_levels(c, den, host_below, stg, S);
+    char* digits_out = to_dec_levels(c, den, host_below, stg, S, len);
     const double t_all = since(t0);
     const double tv[8] = {t_all, t_tree, t_div, t_all - t_tree - t_div, S.gpu_s, S.host_s, (double)S.gpu_products,
                           (double)S.host_products};
     fill_timing(timing, tv, 8);
-    *out = export_str(s, len);
+    *out = digits_out;
     return *out ? NN_OK : NN_ERR_OOM;
   } catch (const std::bad_alloc&) {
     return NN_ERR_OOM;
@@ -774,12 +744,12 @@ nn_status nn_e_dec_levels(nn_context* c, uint64_t terms, uint64_t digits, uint64
     num *= pow(natural(10), digits);
     num /= den;
     const double t_div = since(t0) - t_tree;
-    std::string s = to_dec_levels(c, num, host_below, stg, S);
+    char* digits_out = to_dec_levels(c, num, host_below, stg, S, len);
     const double t_all = since(t0);
     const double tv[8] = {t_all, t_tree, t_div, t_all - t_tree - t_div, S.gpu_s, S.host_s, (double)S.gpu_products,
                           (double)S.host_products};
     fill_timing(timing, tv, 8);
-    *out = export_str(s, len);
+    *out = digits_out;
     return *out ? NN_OK : NN_ERR_OOM;
   } catch (const std::bad_alloc&) {
     return NN_ERR_OOM;
@@ -796,7 +766,7 @@ nn_status nn_to_dec_levels(nn_context* c, const uint64_t* a, uint64_t na, uint64
     const natural x = to_natural(a, na);
     Stats S;
     Staging stg;
-    *out = export_str(to_dec_levels(c, x, host_below, stg, S), len);
+    *out = to_dec_levels(c, x, host_below, stg, S, len);
     return *out ? NN_OK : NN_ERR_OOM;
   } catch (const std::bad_alloc&) {
     return NN_ERR_OOM;

@@ -158,6 +158,30 @@ def test_to_dec_levels_golden(ctx, golden):
         assert sdig(ctx.to_dec_levels(p, host_below=4)) == c["dec"]
 
 
+@pytest.mark.parametrize("host_below", [4, 64, 256])
+def test_to_dec_levels_edges_vs_python(ctx, host_below):
+    """Decimal strings from the split levels and the device leaves against
+    Python's str(): random values of 1 to 5000 limbs, powers of ten and their
+    neighbours at the 18-digit group and split-power boundaries (values whose
+    low groups are all zero, first nodes with leading zeros in their field),
+    powers of two and all-ones limbs."""
+    import sys
+    old = sys.get_int_max_str_digits()
+    sys.set_int_max_str_digits(0)
+    try:
+        vals = []
+        for k, n in enumerate([1, 2, 3, 5, 17, 64, 129, 300, 1000, 5000]):
+            vals.append(_int(limbs(900 + k, n)))
+        for e in [18, 19, 35, 36, 37, 72, 144, 288, 576, 1152, 2304, 4608, 9216, 20000]:
+            vals += [10 ** e - 1, 10 ** e, 10 ** e + 1, 10 ** e * 7 + 3]
+        vals += [2 ** 64, 2 ** 64 - 1, 2 ** 4096, 2 ** 20000 - 1, 10 ** 5000 * (2 ** 64 - 1)]
+        for v in vals:
+            got = ctx.to_dec_levels(_limbs_of(v), host_below=host_below)
+            assert got == str(v), (v.bit_length(), host_below)
+    finally:
+        sys.set_int_max_str_digits(old)
+
+
 @pytest.mark.parametrize("kind", ["pi", "e"])
 def test_levels_1e7_and_1e8_digits(ctx, golden, kind):
     """pi and e to 10^7 and 10^8 digits (the reference's recipes with 2^20 /
