@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(256) pointwise_kernel(u64* dst, const u64* a, 
 // by the same engine.  The 16-column rows are 128 bytes, so the unpadded
 // tile has no bank conflicts (a warp reads two full rows).  SCALE applies
 // the 2^-(s-1) scale in shared memory before the store.
-template <bool INV, bool SCALE, int PR>
+template <bool INV, bool SCALE, int PR, int MAXK>
 __device__ __forceinline__ void col_tile_tma(u64* sm, u64* bar, const CUtensorMap* tm, int s, int lambda0, int R,
                                              const u64* __restrict__ tw, u64 tile, u32* err) {
   constexpr int C = 16;
@@ -167,9 +167,9 @@ __device__ __forceinline__ void col_tile_tma(u64* sm, u64* bar, const CUtensorMa
   }
   mbar_wait(bar, 0);  // completed phase: this thread sees the copied tile
   if (!INV)
-    tile_forward_any<C, PR, true, 3, false>(sm, R, ksb, tw, nullptr, 0);
+    tile_forward_any<C, PR, true, MAXK, false>(sm, R, ksb, tw, nullptr, 0);
   else
-    tile_inverse_any<C, PR, true, 3, false>(sm, R, ksb, tw, nullptr, 0);
+    tile_inverse_any<C, PR, true, MAXK, false>(sm, R, ksb, tw, nullptr, 0);
   if (SCALE) {
     for (u32 idx = 2 * threadIdx.x; idx < nel; idx += 2 * blockDim.x) {
       ulonglong2 v = ld2<false>(sm + idx);
@@ -186,19 +186,20 @@ __device__ __forceinline__ void col_tile_tma(u64* sm, u64* bar, const CUtensorMa
   }
 }
 
-template <bool INV, bool SCALE>
-__global__ void __launch_bounds__(256, 4) ntt_col_tma_kernel(const __grid_constant__ CUtensorMap tm, int s, int lambda0,
+template <bool INV, bool SCALE, int BLOCKS>
+__global__ void __launch_bounds__(256, BLOCKS) ntt_col_tma_kernel(const __grid_constant__ CUtensorMap tm, int s, int lambda0,
                                                           int R, const u64* __restrict__ tab, u64 tab_stride,
                                                           u32* err) {
   extern __shared__ __align__(128) u64 sm[];
   __shared__ __align__(8) u64 bar;
+  constexpr int K = BLOCKS == 3 ? 4 : 3;  // three CTAs an SM leave 80 registers: radix-16 groups
   const u64* tw = tab + blockIdx.y * tab_stride;
   if (blockIdx.y == 0)
-    col_tile_tma<INV, SCALE, 0>(sm, &bar, &tm, s, lambda0, R, tw, blockIdx.x, err);
+    col_tile_tma<INV, SCALE, 0, K>(sm, &bar, &tm, s, lambda0, R, tw, blockIdx.x, err);
   else if (blockIdx.y == 1)
-    col_tile_tma<INV, SCALE, 1>(sm, &bar, &tm, s, lambda0, R, tw, blockIdx.x, err);
+    col_tile_tma<INV, SCALE, 1, K>(sm, &bar, &tm, s, lambda0, R, tw, blockIdx.x, err);
   else
-    col_tile_tma<INV, SCALE, 2>(sm, &bar, &tm, s, lambda0, R, tw, blockIdx.x, err);
+    col_tile_tma<INV, SCALE, 2, K>(sm, &bar, &tm, s, lambda0, R, tw, blockIdx.x, err);
 }
 
 // All threads learn whether the copies of phase `parity` completed: thread 0
@@ -298,7 +299,7 @@ __device__ __forceinline__ void row_tile_bulk(u64* sm, u64* bar, u64* res, const
       tile_inverse_any<C, PR, true, MAXK>(sm, R, ksb, itw, tws, 0);
     }
   } else {
-    tile_inverse_any<C, PR, true>(sm, R, ksb, tw, tws, 0);
+    tile_inverse_any<C, PR, true, MAXK>(sm, R, ksb, tw, tws, 0);
   }
   fence_async_smem();
   __syncthreads();
@@ -306,17 +307,18 @@ __device__ __forceinline__ void row_tile_bulk(u64* sm, u64* bar, u64* res, const
   if (threadIdx.x < nruns) bulk_store_drain();
 }
 
-template <bool INV>
-__global__ void __launch_bounds__(256, 4) ntt_row_bulk_kernel(u64* res, int s, int R, const u64* __restrict__ tab,
-                                                           u64 tab_stride, u32* err) {
+template <bool INV, int BLOCKS>
+__global__ void __launch_bounds__(256, BLOCKS) ntt_row_bulk_kernel(u64* res, int s, int R, const u64* __restrict__ tab,
+                                                                u64 tab_stride, u32* err) {
   extern __shared__ __align__(128) u64 sm[];
   __shared__ __align__(8) u64 bar;
+  constexpr int K = BLOCKS == 3 ? 4 : 3;  // three CTAs an SM leave 80 registers: radix-16 groups
   if (blockIdx.y == 0)
-    row_tile_bulk<INV, false, 0, 3>(sm, &bar, res, nullptr, s, R, tab, nullptr, tab_stride, blockIdx.x, err);
+    row_tile_bulk<INV, false, 0, K>(sm, &bar, res, nullptr, s, R, tab, nullptr, tab_stride, blockIdx.x, err);
   else if (blockIdx.y == 1)
-    row_tile_bulk<INV, false, 1, 3>(sm, &bar, res, nullptr, s, R, tab, nullptr, tab_stride, blockIdx.x, err);
+    row_tile_bulk<INV, false, 1, K>(sm, &bar, res, nullptr, s, R, tab, nullptr, tab_stride, blockIdx.x, err);
   else
-    row_tile_bulk<INV, false, 2, 3>(sm, &bar, res, nullptr, s, R, tab, nullptr, tab_stride, blockIdx.x, err);
+    row_tile_bulk<INV, false, 2, K>(sm, &bar, res, nullptr, s, R, tab, nullptr, tab_stride, blockIdx.x, err);
 }
 
 // The fused last pass with bulk copies; register budgets as ntt_fused_kernel.
@@ -378,20 +380,46 @@ bool col_tensor_map(CUtensorMap* m, const u64* res, int s, int lambda0, int R) {
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <bool INV, bool SCALE>
-cudaError_t launch_col_tma(const CUtensorMap& tm, int s, const Pass& ps, const Tables& t, cudaStream_t st) {
+template <bool INV, bool SCALE, int BLOCKS>
+cudaError_t launch_col_tma_b(const CUtensorMap& tm, int s, const Pass& ps, const Tables& t, cudaStream_t st) {
   const size_t smem = ((size_t)16 << ps.R) * 8;
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(ntt_col_tma_kernel<INV, SCALE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         200 * 1024);
+    cudaError_t e = cudaFuncSetAttribute(ntt_col_tma_kernel<INV, SCALE, BLOCKS>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (e != cudaSuccess) return e;
     configured = true;
   }
   const u64 tiles = (1ull << s) / ((u64)16 << ps.R);
   launch_begin(INV ? (SCALE ? "ntt_inv_last_col_pass" : "ntt_inv_col_pass") : "ntt_fwd_col_pass", st);
-  ntt_col_tma_kernel<INV, SCALE><<<dim3((unsigned)tiles, 3), 256, smem, st>>>(tm, s, ps.lambda0, ps.R,
-                                                                              INV ? t.iroot : t.root, t.cap, t.err);
+  ntt_col_tma_kernel<INV, SCALE, BLOCKS><<<dim3((unsigned)tiles, 3), 256, smem, st>>>(
+      tm, s, ps.lambda0, ps.R, INV ? t.iroot : t.root, t.cap, t.err);
+  launch_end(st);
+  return cudaGetLastError();
+}
+
+// Four CTAs an SM: radix-16 groups (three CTAs, 80 registers) spill in the
+// column passes, whose twiddle pairs stay in registers, and measured slower
+// (2^27 multiply 50.4 -> 52.4 ms).
+template <bool INV, bool SCALE>
+cudaError_t launch_col_tma(const CUtensorMap& tm, int s, const Pass& ps, const Tables& t, cudaStream_t st) {
+  return launch_col_tma_b<INV, SCALE, 4>(tm, s, ps, t, st);
+}
+
+template <bool INV, int BLOCKS>
+cudaError_t launch_row_bulk(u64* out, int s, const Pass& ps, const Tables& t, cudaStream_t st) {
+  const size_t smem = tile_smem_bytes(2, ps.R);
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(ntt_row_bulk_kernel<INV, BLOCKS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         200 * 1024);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  const u64 tiles = (1ull << s) / ((u64)2 << ps.R);
+  launch_begin(INV ? "ntt_inv_row_pass" : "ntt_fwd_row_pass", st);
+  ntt_row_bulk_kernel<INV, BLOCKS><<<dim3((unsigned)tiles, 3), 256, smem, st>>>(out, s, ps.R, INV ? t.iroot : t.root,
+                                                                                 t.cap, t.err);
   launch_end(st);
   return cudaGetLastError();
 }
@@ -404,20 +432,9 @@ cudaError_t launch_pass(const u64* in, u64* out, u64 n_in, int s, const Pass& ps
   }
   if constexpr (C == 2 && !FIRST && !SCALE) {
     if (in == out && aligned16(out) && ps.lambda0 + ps.R == s - 1) {
-      const size_t smem = tile_smem_bytes(2, ps.R);
-      static bool configured = false;
-      if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(ntt_row_bulk_kernel<INV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             200 * 1024);
-        if (e != cudaSuccess) return e;
-        configured = true;
-      }
-      const u64 tiles = (1ull << s) / ((u64)2 << ps.R);
-      launch_begin(INV ? "ntt_inv_row_pass" : "ntt_fwd_row_pass", st);
-      ntt_row_bulk_kernel<INV><<<dim3((unsigned)tiles, 3), 256, smem, st>>>(out, s, ps.R, INV ? t.iroot : t.root,
-                                                                             t.cap, t.err);
-      launch_end(st);
-      return cudaGetLastError();
+      // tiles that leave room for three CTAs an SM only get 80 registers and radix-16 groups
+      if (4 * tile_smem_bytes(2, ps.R) > 227 * 1024) return launch_row_bulk<INV, 3>(out, s, ps, t, st);
+      return launch_row_bulk<INV, 4>(out, s, ps, t, st);
     }
   }
   const size_t smem = tile_smem_bytes(ps.C, ps.R);

@@ -277,7 +277,7 @@ __device__ __forceinline__ void tile_forward_any(u64* sm, int R, u64 ksb, const 
     if (R == 11 && l0 == 0) return tile_forward_ct<C, PR, 11, 0, MAXK, PAD>(sm, ksb, tw, tws);
     if (R == 10 && l0 == 0) return tile_forward_ct<C, PR, 10, 0, 3, PAD>(sm, ksb, tw, tws);
   } else if constexpr (CT && C == 16) {
-    if (R == 8 && l0 == 0) return tile_forward_ct<C, PR, 8, 0, 3, PAD>(sm, ksb, tw, tws);
+    if (R == 8 && l0 == 0) return tile_forward_ct<C, PR, 8, 0, MAXK, PAD>(sm, ksb, tw, tws);
     if (R == 8 && l0 == 1) return tile_forward_ct<C, PR, 8, 1, 3, PAD>(sm, ksb, tw, tws);
     if (R == 9 && l0 == 0) return tile_forward_ct<C, PR, 9, 0, 3, PAD>(sm, ksb, tw, tws);
     if (R == 9 && l0 == 1) return tile_forward_ct<C, PR, 9, 1, 3, PAD>(sm, ksb, tw, tws);
@@ -292,7 +292,7 @@ __device__ __forceinline__ void tile_inverse_any(u64* sm, int R, u64 ksb, const 
     if (R == 11 && l_stop == 0) return tile_inverse_ct<C, PR, 11, 0, MAXK, PAD>(sm, ksb, tw, tws);
     if (R == 10 && l_stop == 0) return tile_inverse_ct<C, PR, 10, 0, 3, PAD>(sm, ksb, tw, tws);
   } else if constexpr (CT && C == 16) {
-    if (R == 8 && l_stop == 0) return tile_inverse_ct<C, PR, 8, 0, 3, PAD>(sm, ksb, tw, tws);
+    if (R == 8 && l_stop == 0) return tile_inverse_ct<C, PR, 8, 0, MAXK, PAD>(sm, ksb, tw, tws);
     if (R == 9 && l_stop == 0) return tile_inverse_ct<C, PR, 9, 0, 3, PAD>(sm, ksb, tw, tws);
     if (R == 7 && l_stop == 0) return tile_inverse_ct<C, PR, 7, 0, 3, PAD>(sm, ksb, tw, tws);
   }
