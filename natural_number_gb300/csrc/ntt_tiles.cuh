@@ -349,24 +349,43 @@ __device__ __forceinline__ void pass_tile_p(u64* sm, const u64* in, u64* out, u6
   if (FIRST) {
     const bool vec = ((reinterpret_cast<unsigned long long>(in) & 15) == 0);
     const u32 nload = half ? nel / 2 : nel;
-    for (u32 idx = 2 * threadIdx.x; idx < nload; idx += 2 * blockDim.x) {
-      const u64 pos = base + ((u64)(idx >> LGC) << lg_s) + (idx & (C - 1));
-      u64 x0 = 0, x1 = 0;
-      if (vec && pos + 1 < n_in) {
-        const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(in + pos);
-        x0 = v.x;
-        x1 = v.y;
-      } else {
-        if (pos < n_in) x0 = in[pos];
-        if (pos + 1 < n_in) x1 = in[pos + 1];
+    // kLoadBatch pairs of limbs a thread are loaded before any is reduced, so
+    // their latencies overlap (the compiler keeps generic loads in order with
+    // the shared-memory stores between them)
+    constexpr int kLoadBatch = 4;
+    for (u32 idx0 = 2 * threadIdx.x; idx0 < nload; idx0 += 2 * kLoadBatch * blockDim.x) {
+      u64 x0[kLoadBatch], x1[kLoadBatch];
+#pragma unroll
+      for (int b = 0; b < kLoadBatch; ++b) {
+        const u32 idx = idx0 + 2 * b * blockDim.x;
+        const u64 pos = base + ((u64)(idx >> LGC) << lg_s) + (idx & (C - 1));
+        x0[b] = 0;
+        x1[b] = 0;
+        if (idx < nload) {
+          if (vec && pos + 1 < n_in) {
+            const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(in + pos);
+            x0[b] = v.x;
+            x1[b] = v.y;
+          } else {
+            if (pos < n_in) x0[b] = in[pos];
+            if (pos + 1 < n_in) x1[b] = in[pos + 1];
+          }
+        }
       }
-      const u64 r0 = pos < n_in ? limb_mod(x0, PrimeC<PR>::m64, p, ch) : 0;
-      const u64 r1 = pos + 1 < n_in ? limb_mod(x1, PrimeC<PR>::m64, p, ch) : 0;
-      sm[pad16(idx)] = r0;
-      sm[pad16(idx + 1)] = r1;
-      if (half) {
-        sm[pad16(idx + nload)] = r0;
-        sm[pad16(idx + nload + 1)] = r1;
+#pragma unroll
+      for (int b = 0; b < kLoadBatch; ++b) {
+        const u32 idx = idx0 + 2 * b * blockDim.x;
+        if (idx < nload) {
+          const u64 pos = base + ((u64)(idx >> LGC) << lg_s) + (idx & (C - 1));
+          const u64 r0 = pos < n_in ? limb_mod(x0[b], PrimeC<PR>::m64, p, ch) : 0;
+          const u64 r1 = pos + 1 < n_in ? limb_mod(x1[b], PrimeC<PR>::m64, p, ch) : 0;
+          sm[pad16(idx)] = r0;
+          sm[pad16(idx + 1)] = r1;
+          if (half) {
+            sm[pad16(idx + nload)] = r0;
+            sm[pad16(idx + nload + 1)] = r1;
+          }
+        }
       }
     }
   } else {
