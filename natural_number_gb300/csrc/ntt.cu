@@ -202,6 +202,46 @@ __global__ void __launch_bounds__(256, BLOCKS) ntt_col_tma_kernel(const __grid_c
     col_tile_tma<INV, SCALE, 2, K>(sm, &bar, &tm, s, lambda0, R, tw, blockIdx.x, err);
 }
 
+// The first pass (levels [0, R) from limbs) with a bulk store: the tile (16
+// columns x 2^R rows of one prime, dense 128-byte rows) is filled from the
+// limbs by the threads, reduced mod p on the way, and goes back to the
+// residues as the same tensor-map boxes as a strided pass's tile.  CTAs are
+// numbered prime-fastest (x = 3 * tile + prime): the three CTAs that read the
+// same limbs run together, so the limbs cross HBM about once.
+template <int PR>
+__device__ __forceinline__ void load_tile_tma(u64* sm, const CUtensorMap* tm, const u64* in, u64 n_in, int s, int R,
+                                              const u64* __restrict__ tw, u64 tile) {
+  constexpr int C = 16;
+  const int lg_s = s - R;
+  const u64 base = tile * C;  // one super-block at level 0: the tile's first column
+  const u32 rows = 1u << R, nel = (u32)C << R, box_rows = rows < 256 ? rows : 256;
+  const bool half = n_in <= (1ull << (s - 1));
+  load_limbs_tile<C, PR, false>(sm, in, n_in, base, lg_s, half ? nel / 2 : nel, half);
+  __syncthreads();
+  tile_forward_any<C, PR, true, 3, false>(sm, R, 0, tw, nullptr, half ? 1 : 0);
+  fence_async_smem();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (u32 y = 0; y < rows; y += box_rows) tma_store_3d(tm, (int)base, (int)y, PR, sm + (u64)y * C);
+    bulk_store_drain();
+  }
+}
+
+__global__ void __launch_bounds__(256, 4) ntt_load_tma_kernel(const __grid_constant__ CUtensorMap tm, const u64* in,
+                                                           u64 n_in, int s, int R, const u64* __restrict__ tab,
+                                                           u64 tab_stride) {
+  extern __shared__ __align__(128) u64 sm[];
+  const int prime = (int)(blockIdx.x % 3);
+  const u64 tile = blockIdx.x / 3;
+  const u64* tw = tab + prime * tab_stride;
+  if (prime == 0)
+    load_tile_tma<0>(sm, &tm, in, n_in, s, R, tw, tile);
+  else if (prime == 1)
+    load_tile_tma<1>(sm, &tm, in, n_in, s, R, tw, tile);
+  else
+    load_tile_tma<2>(sm, &tm, in, n_in, s, R, tw, tile);
+}
+
 // All threads learn whether the copies of phase `parity` completed: thread 0
 // waits (bounded), the others then observe the completed phase, which makes
 // the copied bytes visible to them.  A wait that ran out is recorded in *err;
@@ -429,6 +469,24 @@ cudaError_t launch_pass(const u64* in, u64* out, u64 n_in, int s, const Pass& ps
   if constexpr (C == 16 && !FIRST) {
     CUtensorMap tm;
     if (in == out && col_tensor_map(&tm, out, s, ps.lambda0, ps.R)) return launch_col_tma<INV, SCALE>(tm, s, ps, t, st);
+  }
+  if constexpr (C == 16 && FIRST && !INV) {
+    CUtensorMap tm;
+    if (ps.lambda0 == 0 && col_tensor_map(&tm, out, s, 0, ps.R)) {
+      const size_t smem = ((size_t)16 << ps.R) * 8;
+      static bool configured = false;
+      if (!configured) {
+        cudaError_t e =
+            cudaFuncSetAttribute(ntt_load_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        if (e != cudaSuccess) return e;
+        configured = true;
+      }
+      const u64 tiles = (1ull << s) / ((u64)16 << ps.R);
+      launch_begin("ntt_fwd_load_col_pass", st);
+      ntt_load_tma_kernel<<<(unsigned)(3 * tiles), 256, smem, st>>>(tm, in, n_in, s, ps.R, t.root, t.cap);
+      launch_end(st);
+      return cudaGetLastError();
+    }
   }
   if constexpr (C == 2 && !FIRST && !SCALE) {
     if (in == out && aligned16(out) && ps.lambda0 + ps.R == s - 1) {

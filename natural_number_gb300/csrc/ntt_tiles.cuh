@@ -305,7 +305,6 @@ __device__ __forceinline__ void tile_inverse_any(u64* sm, int R, u64 ksb, const 
 template <int PR>
 __device__ __forceinline__ void pointwise4(u64 (&o)[4], const u64 (&A)[4], const u64 (&Bv)[4], ulonglong2 wv) {
   constexpr u64 p = PrimeC<PR>::p;
-  constexpr u32 ch = PrimeC<PR>::c_hi;
   const u64 a0 = canon_c<PR>(A[0]), a1 = canon_c<PR>(A[1]), a2 = canon_c<PR>(A[2]), a3 = canon_c<PR>(A[3]);
   const u64 b0 = canon_c<PR>(Bv[0]), b1 = canon_c<PR>(Bv[1]), b2 = canon_c<PR>(Bv[2]), b3 = canon_c<PR>(Bv[3]);
   const u64 wb1 = shoup_mul_c<PR>(b1, wv.x, wv.y);
@@ -315,6 +314,60 @@ __device__ __forceinline__ void pointwise4(u64 (&o)[4], const u64 (&A)[4], const
   o[1] = barrett_c<PR>(add128(mul_wide(a0, b1), mul_wide(a1, b0)));
   o[2] = barrett_c<PR>(add128(mul_wide(a2, b2), mul_wide(a3, nwb3)));
   o[3] = barrett_c<PR>(add128(mul_wide(a2, b3), mul_wide(a3, b2)));
+}
+
+// The first pass's tile from limbs: element idx < nload (row idx / C, column
+// idx % C) is limb base + row * 2^lg_s + column reduced mod p (zero at and
+// beyond n_in); with `half`, every limb lies in the lower half of the
+// transform and level 0 pairs it with a zero, so its residue also goes to
+// element idx + nload.  PAD: the padded shared layout (pad16), else dense.
+// kLoadBatch pairs of limbs a thread are loaded before any is reduced, so
+// their latencies overlap (the compiler keeps generic loads in order with the
+// shared-memory stores between them).
+template <int C, int PR, bool PAD>
+__device__ __forceinline__ void load_limbs_tile(u64* sm, const u64* in, u64 n_in, u64 base, int lg_s, u32 nload,
+                                                bool half) {
+  constexpr u64 p = PrimeC<PR>::p;
+  constexpr u32 ch = PrimeC<PR>::c_hi;
+  constexpr int LGC = C == 2 ? 1 : C == 16 ? 4 : C == 32 ? 5 : C == 64 ? 6 : 7;
+  constexpr int kLoadBatch = 4;
+  auto at = [](u32 i) { return PAD ? pad16(i) : i; };
+  const bool vec = ((reinterpret_cast<unsigned long long>(in) & 15) == 0);
+  for (u32 idx0 = 2 * threadIdx.x; idx0 < nload; idx0 += 2 * kLoadBatch * blockDim.x) {
+    u64 x0[kLoadBatch], x1[kLoadBatch];
+#pragma unroll
+    for (int b = 0; b < kLoadBatch; ++b) {
+      const u32 idx = idx0 + 2 * b * blockDim.x;
+      const u64 pos = base + ((u64)(idx >> LGC) << lg_s) + (idx & (C - 1));
+      x0[b] = 0;
+      x1[b] = 0;
+      if (idx < nload) {
+        if (vec && pos + 1 < n_in) {
+          const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(in + pos);
+          x0[b] = v.x;
+          x1[b] = v.y;
+        } else {
+          if (pos < n_in) x0[b] = in[pos];
+          if (pos + 1 < n_in) x1[b] = in[pos + 1];
+        }
+      }
+    }
+#pragma unroll
+    for (int b = 0; b < kLoadBatch; ++b) {
+      const u32 idx = idx0 + 2 * b * blockDim.x;
+      if (idx < nload) {
+        const u64 pos = base + ((u64)(idx >> LGC) << lg_s) + (idx & (C - 1));
+        const u64 r0 = pos < n_in ? limb_mod(x0[b], PrimeC<PR>::m64, p, ch) : 0;
+        const u64 r1 = pos + 1 < n_in ? limb_mod(x1[b], PrimeC<PR>::m64, p, ch) : 0;
+        sm[at(idx)] = r0;
+        sm[at(idx + 1)] = r1;
+        if (half) {
+          sm[at(idx + nload)] = r0;
+          sm[at(idx + nload + 1)] = r1;
+        }
+      }
+    }
+  }
 }
 
 // One tile of a pass over levels [lambda0, lambda0+R): C columns x 2^R rows of
@@ -331,7 +384,6 @@ __device__ __forceinline__ void pass_tile_p(u64* sm, const u64* in, u64* out, u6
                                             const u64* __restrict__ tab, const u64* __restrict__ itab, u64 tab_stride,
                                             u64 tile, const u64* other, int skip) {
   constexpr u64 p = PrimeC<PR>::p;
-  constexpr u32 ch = PrimeC<PR>::c_hi;
   const u64 L = 1ull << s;
   const u64* tw = tab + (u64)PR * tab_stride;
   const int lg_s = s - lambda0 - R;
@@ -347,47 +399,7 @@ __device__ __forceinline__ void pass_tile_p(u64* sm, const u64* in, u64* out, u6
   // at once, and the tile starts at level 1.
   const bool half = FIRST && lambda0 == 0 && n_in <= (L >> 1);
   if (FIRST) {
-    const bool vec = ((reinterpret_cast<unsigned long long>(in) & 15) == 0);
-    const u32 nload = half ? nel / 2 : nel;
-    // kLoadBatch pairs of limbs a thread are loaded before any is reduced, so
-    // their latencies overlap (the compiler keeps generic loads in order with
-    // the shared-memory stores between them)
-    constexpr int kLoadBatch = 4;
-    for (u32 idx0 = 2 * threadIdx.x; idx0 < nload; idx0 += 2 * kLoadBatch * blockDim.x) {
-      u64 x0[kLoadBatch], x1[kLoadBatch];
-#pragma unroll
-      for (int b = 0; b < kLoadBatch; ++b) {
-        const u32 idx = idx0 + 2 * b * blockDim.x;
-        const u64 pos = base + ((u64)(idx >> LGC) << lg_s) + (idx & (C - 1));
-        x0[b] = 0;
-        x1[b] = 0;
-        if (idx < nload) {
-          if (vec && pos + 1 < n_in) {
-            const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(in + pos);
-            x0[b] = v.x;
-            x1[b] = v.y;
-          } else {
-            if (pos < n_in) x0[b] = in[pos];
-            if (pos + 1 < n_in) x1[b] = in[pos + 1];
-          }
-        }
-      }
-#pragma unroll
-      for (int b = 0; b < kLoadBatch; ++b) {
-        const u32 idx = idx0 + 2 * b * blockDim.x;
-        if (idx < nload) {
-          const u64 pos = base + ((u64)(idx >> LGC) << lg_s) + (idx & (C - 1));
-          const u64 r0 = pos < n_in ? limb_mod(x0[b], PrimeC<PR>::m64, p, ch) : 0;
-          const u64 r1 = pos + 1 < n_in ? limb_mod(x1[b], PrimeC<PR>::m64, p, ch) : 0;
-          sm[pad16(idx)] = r0;
-          sm[pad16(idx + 1)] = r1;
-          if (half) {
-            sm[pad16(idx + nload)] = r0;
-            sm[pad16(idx + nload + 1)] = r1;
-          }
-        }
-      }
-    }
+    load_limbs_tile<C, PR, true>(sm, in, n_in, base, lg_s, half ? nel / 2 : nel, half);
   } else {
     const u64* src = in + (u64)PR * L;
     for (u32 idx = 2 * threadIdx.x; idx < nel; idx += 2 * blockDim.x) {
