@@ -138,7 +138,8 @@ __global__ void __launch_bounds__(256) pointwise_kernel(u64* dst, const u64* a, 
 // loaded by one thread onto an mbarrier and stored back from shared memory
 // by the same engine.  The 16-column rows are 128 bytes, so the unpadded
 // tile has no bank conflicts (a warp reads two full rows).  SCALE applies
-// the 2^-(s-1) scale in shared memory before the store.
+// the 2^-(s-1) scale: in the last register group where the tile shape has a
+// compile-time schedule, else in shared memory before the store.
 template <bool INV, bool SCALE, int PR, int MAXK>
 __device__ __forceinline__ void col_tile_tma(u64* sm, u64* bar, const CUtensorMap* tm, int s, int lambda0, int R,
                                              const u64* __restrict__ tw, u64 tile, u32* err) {
@@ -166,11 +167,12 @@ __device__ __forceinline__ void col_tile_tma(u64* sm, u64* bar, const CUtensorMa
     return;
   }
   mbar_wait(bar, 0);  // completed phase: this thread sees the copied tile
+  bool scaled = false;  // the compile-time schedules scale in their last register group
   if (!INV)
     tile_forward_any<C, PR, true, MAXK, false>(sm, R, ksb, tw, nullptr, 0);
   else
-    tile_inverse_any<C, PR, true, MAXK, false>(sm, R, ksb, tw, nullptr, 0);
-  if (SCALE) {
+    scaled = tile_inverse_any<C, PR, true, MAXK, false, SCALE>(sm, R, ksb, tw, nullptr, 0, (u32)(s - 1));
+  if (SCALE && !scaled) {
     for (u32 idx = 2 * threadIdx.x; idx < nel; idx += 2 * blockDim.x) {
       ulonglong2 v = ld2<false>(sm + idx);
       v.x = div_pow2(canon_c<PR>(v.x), (u32)(s - 1), p);

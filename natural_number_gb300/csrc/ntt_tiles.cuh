@@ -124,9 +124,10 @@ __device__ __forceinline__ void stage_twiddles(u64* tws, const u64* tw, u64 ksb,
 // unit's rows are S = C * 2^nsub words apart, and the padded index is linear
 // in the row: pad16(x0 + m*S) = pad16(x0) + m*S + 2*floor(m*S/32) for every
 // unit of every tile shape used here, so each row is one add from the first.
-template <int K, int C, bool INV, int PR, bool PAD = true>
+// SC (inverse only): the group also scales its outputs by 2^-sc_sh to [0, p).
+template <int K, int C, bool INV, int PR, bool PAD = true, bool SC = false>
 __device__ __forceinline__ void level_group(u64* sm, int l, int R, u64 ksb, const u64* __restrict__ tw,
-                                            const u64* tws) {
+                                            const u64* tws, u32 sc_sh = 0) {
   const int nsub = R - l - K;
   const u32 units = (u32)C << (R - K);
   const u32 tmask = (1u << nsub) - 1;
@@ -170,6 +171,10 @@ __device__ __forceinline__ void level_group(u64* sm, int l, int R, u64 ksb, cons
 #pragma unroll
           for (int m = 0; m < half; ++m) inv_bfly_c<PR>(x[g * 2 * half + m], x[g * 2 * half + m + half], wv.x, wv.y);
         }
+      }
+      if constexpr (SC) {
+#pragma unroll
+        for (int m = 0; m < (1 << K); ++m) x[m] = div_pow2(canon_c<PR>(x[m]), sc_sh, PrimeC<PR>::p);
       }
     }
 #pragma unroll
@@ -251,19 +256,20 @@ __device__ __forceinline__ void tile_inverse(u64* sm, int R, u64 ksb, const u64*
   }
 }
 // Inverse groups from level L (exclusive) down to LSTOP.
-template <int C, int PR, int R, int L, int LSTOP, int N, int G, bool PAD = true>
-__device__ __forceinline__ void inv_groups_ct(u64* sm, u64 ksb, const u64* tw, const u64* tws) {
+// SC: the last group also applies the scale 2^-sc_sh.
+template <int C, int PR, int R, int L, int LSTOP, int N, int G, bool PAD = true, bool SC = false>
+__device__ __forceinline__ void inv_groups_ct(u64* sm, u64 ksb, const u64* tw, const u64* tws, u32 sc_sh) {
   if constexpr (G < N) {
     constexpr int K = (L - LSTOP + (N - G) - 1) / (N - G);
-    level_group<K, C, true, PR, PAD>(sm, L - K, R, ksb, tw, tws);
+    level_group<K, C, true, PR, PAD, SC && G + 1 == N>(sm, L - K, R, ksb, tw, tws, sc_sh);
     __syncthreads();
-    inv_groups_ct<C, PR, R, L - K, LSTOP, N, G + 1, PAD>(sm, ksb, tw, tws);
+    inv_groups_ct<C, PR, R, L - K, LSTOP, N, G + 1, PAD, SC>(sm, ksb, tw, tws, sc_sh);
   }
 }
-template <int C, int PR, int R, int LSTOP, int MAXK = 3, bool PAD = true>
-__device__ __forceinline__ void tile_inverse_ct(u64* sm, u64 ksb, const u64* tw, const u64* tws) {
+template <int C, int PR, int R, int LSTOP, int MAXK = 3, bool PAD = true, bool SC = false>
+__device__ __forceinline__ void tile_inverse_ct(u64* sm, u64 ksb, const u64* tw, const u64* tws, u32 sc_sh = 0) {
   constexpr int cap = group_cap_ct(C, R, MAXK);
-  inv_groups_ct<C, PR, R, R, LSTOP, (R - LSTOP + cap - 1) / cap, 0, PAD>(sm, ksb, tw, tws);
+  inv_groups_ct<C, PR, R, R, LSTOP, (R - LSTOP + cap - 1) / cap, 0, PAD, SC>(sm, ksb, tw, tws, sc_sh);
 }
 
 // Forward levels [l0, R) / inverse levels R-1 .. l_stop: the compile-time
@@ -286,17 +292,22 @@ __device__ __forceinline__ void tile_forward_any(u64* sm, int R, u64 ksb, const 
   }
   tile_forward<C, PR, PAD>(sm, R, ksb, tw, tws, l0);
 }
-template <int C, int PR, bool CT, int MAXK = 3, bool PAD = true>
-__device__ __forceinline__ void tile_inverse_any(u64* sm, int R, u64 ksb, const u64* tw, const u64* tws, int l_stop) {
+// SC: a compile-time schedule also applies the scale 2^-sc_sh in its last
+// group; returns whether it did (the runtime loop leaves the scale to the
+// caller).
+template <int C, int PR, bool CT, int MAXK = 3, bool PAD = true, bool SC = false>
+__device__ __forceinline__ bool tile_inverse_any(u64* sm, int R, u64 ksb, const u64* tw, const u64* tws, int l_stop,
+                                                 u32 sc_sh = 0) {
   if constexpr (CT && C == 2) {
-    if (R == 11 && l_stop == 0) return tile_inverse_ct<C, PR, 11, 0, MAXK, PAD>(sm, ksb, tw, tws);
-    if (R == 10 && l_stop == 0) return tile_inverse_ct<C, PR, 10, 0, 3, PAD>(sm, ksb, tw, tws);
+    if (R == 11 && l_stop == 0) return tile_inverse_ct<C, PR, 11, 0, MAXK, PAD, SC>(sm, ksb, tw, tws, sc_sh), SC;
+    if (R == 10 && l_stop == 0) return tile_inverse_ct<C, PR, 10, 0, 3, PAD, SC>(sm, ksb, tw, tws, sc_sh), SC;
   } else if constexpr (CT && C == 16) {
-    if (R == 8 && l_stop == 0) return tile_inverse_ct<C, PR, 8, 0, MAXK, PAD>(sm, ksb, tw, tws);
-    if (R == 9 && l_stop == 0) return tile_inverse_ct<C, PR, 9, 0, 3, PAD>(sm, ksb, tw, tws);
-    if (R == 7 && l_stop == 0) return tile_inverse_ct<C, PR, 7, 0, 3, PAD>(sm, ksb, tw, tws);
+    if (R == 8 && l_stop == 0) return tile_inverse_ct<C, PR, 8, 0, MAXK, PAD, SC>(sm, ksb, tw, tws, sc_sh), SC;
+    if (R == 9 && l_stop == 0) return tile_inverse_ct<C, PR, 9, 0, 3, PAD, SC>(sm, ksb, tw, tws, sc_sh), SC;
+    if (R == 7 && l_stop == 0) return tile_inverse_ct<C, PR, 7, 0, 3, PAD, SC>(sm, ksb, tw, tws, sc_sh), SC;
   }
   tile_inverse<C, PR, PAD>(sm, R, ksb, tw, tws, l_stop);
+  return false;
 }
 
 // Pointwise product of one group of 4 residues (a0..a3)(b0..b3), lazy forward
