@@ -188,8 +188,8 @@ __device__ __forceinline__ void col_tile_tma(u64* sm, u64* bar, const CUtensorMa
   }
 }
 
-template <bool INV, bool SCALE, int BLOCKS>
-__global__ void __launch_bounds__(256, BLOCKS) ntt_col_tma_kernel(const __grid_constant__ CUtensorMap tm, int s, int lambda0,
+template <bool INV, bool SCALE, int BLOCKS, int THREADS = 256>
+__global__ void __launch_bounds__(THREADS, BLOCKS) ntt_col_tma_kernel(const __grid_constant__ CUtensorMap tm, int s, int lambda0,
                                                           int R, const u64* __restrict__ tab, u64 tab_stride,
                                                           u32* err) {
   extern __shared__ __align__(128) u64 sm[];
@@ -229,7 +229,8 @@ __device__ __forceinline__ void load_tile_tma(u64* sm, const CUtensorMap* tm, co
   }
 }
 
-__global__ void __launch_bounds__(256, 4) ntt_load_tma_kernel(const __grid_constant__ CUtensorMap tm, const u64* in,
+template <int BLOCKS, int THREADS>
+__global__ void __launch_bounds__(THREADS, BLOCKS) ntt_load_tma_kernel(const __grid_constant__ CUtensorMap tm, const u64* in,
                                                            u64 n_in, int s, int R, const u64* __restrict__ tab,
                                                            u64 tab_stride) {
   extern __shared__ __align__(128) u64 sm[];
@@ -422,29 +423,33 @@ bool col_tensor_map(CUtensorMap* m, const u64* res, int s, int lambda0, int R) {
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <bool INV, bool SCALE, int BLOCKS>
+template <bool INV, bool SCALE, int BLOCKS, int THREADS = 256>
 cudaError_t launch_col_tma_b(const CUtensorMap& tm, int s, const Pass& ps, const Tables& t, cudaStream_t st) {
   const size_t smem = ((size_t)16 << ps.R) * 8;
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(ntt_col_tma_kernel<INV, SCALE, BLOCKS>,
+    cudaError_t e = cudaFuncSetAttribute(ntt_col_tma_kernel<INV, SCALE, BLOCKS, THREADS>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (e != cudaSuccess) return e;
     configured = true;
   }
   const u64 tiles = (1ull << s) / ((u64)16 << ps.R);
   launch_begin(INV ? (SCALE ? "ntt_inv_last_col_pass" : "ntt_inv_col_pass") : "ntt_fwd_col_pass", st);
-  ntt_col_tma_kernel<INV, SCALE, BLOCKS><<<dim3((unsigned)tiles, 3), 256, smem, st>>>(
+  ntt_col_tma_kernel<INV, SCALE, BLOCKS, THREADS><<<dim3((unsigned)tiles, 3), THREADS, smem, st>>>(
       tm, s, ps.lambda0, ps.R, INV ? t.iroot : t.root, t.cap, t.err);
   launch_end(st);
   return cudaGetLastError();
 }
 
-// Four CTAs an SM: radix-16 groups (three CTAs, 80 registers) spill in the
-// column passes, whose twiddle pairs stay in registers, and measured slower
-// (2^27 multiply 50.4 -> 52.4 ms).
+// Radix-8 groups at 64 registers: radix-16 groups (three CTAs, 80 registers)
+// spill in the column passes, whose twiddle pairs stay in registers, and
+// measured slower (2^27 multiply 50.4 -> 52.4 ms).  Tiles of up to 2^8 rows
+// (32 KiB) run as CTAs of 128 threads, six an SM: a barrier between register
+// groups then waits for four warps instead of eight (2^27 column passes 3-4 %
+// faster than 256-thread CTAs, four an SM).
 template <bool INV, bool SCALE>
 cudaError_t launch_col_tma(const CUtensorMap& tm, int s, const Pass& ps, const Tables& t, cudaStream_t st) {
+  if (ps.R <= 8) return launch_col_tma_b<INV, SCALE, 8, 128>(tm, s, ps, t, st);
   return launch_col_tma_b<INV, SCALE, 4>(tm, s, ps, t, st);
 }
 
@@ -466,6 +471,25 @@ cudaError_t launch_row_bulk(u64* out, int s, const Pass& ps, const Tables& t, cu
   return cudaGetLastError();
 }
 
+template <int BLOCKS, int THREADS>
+cudaError_t launch_load_tma(const CUtensorMap& tm, const u64* in, u64 n_in, int s, const Pass& ps, const Tables& t,
+                            cudaStream_t st) {
+  const size_t smem = ((size_t)16 << ps.R) * 8;
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(ntt_load_tma_kernel<BLOCKS, THREADS>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  const u64 tiles = (1ull << s) / ((u64)16 << ps.R);
+  launch_begin("ntt_fwd_load_col_pass", st);
+  ntt_load_tma_kernel<BLOCKS, THREADS><<<(unsigned)(3 * tiles), THREADS, smem, st>>>(tm, in, n_in, s, ps.R, t.root,
+                                                                                     t.cap);
+  launch_end(st);
+  return cudaGetLastError();
+}
+
 template <int C, bool FIRST, bool INV, bool SCALE>
 cudaError_t launch_pass(const u64* in, u64* out, u64 n_in, int s, const Pass& ps, const Tables& t, cudaStream_t st) {
   if constexpr (C == 16 && !FIRST) {
@@ -475,19 +499,9 @@ cudaError_t launch_pass(const u64* in, u64* out, u64 n_in, int s, const Pass& ps
   if constexpr (C == 16 && FIRST && !INV) {
     CUtensorMap tm;
     if (ps.lambda0 == 0 && col_tensor_map(&tm, out, s, 0, ps.R)) {
-      const size_t smem = ((size_t)16 << ps.R) * 8;
-      static bool configured = false;
-      if (!configured) {
-        cudaError_t e =
-            cudaFuncSetAttribute(ntt_load_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        if (e != cudaSuccess) return e;
-        configured = true;
-      }
-      const u64 tiles = (1ull << s) / ((u64)16 << ps.R);
-      launch_begin("ntt_fwd_load_col_pass", st);
-      ntt_load_tma_kernel<<<(unsigned)(3 * tiles), 256, smem, st>>>(tm, in, n_in, s, ps.R, t.root, t.cap);
-      launch_end(st);
-      return cudaGetLastError();
+      // 256 threads, four CTAs an SM: as 128-thread CTAs the pass measured
+      // slower (2^27 load passes 8.52 -> 9.03 ms), unlike the strided passes
+      return launch_load_tma<4, 256>(tm, in, n_in, s, ps, t, st);
     }
   }
   if constexpr (C == 2 && !FIRST && !SCALE) {
