@@ -16,6 +16,39 @@ struct W3 {
   u64 w0, w1, w2;
 };
 
+// Multiword sums as carry chains (add.cc / addc, mad.lo.cc / madc): the carry
+// travels in the condition code instead of a compare and a select per word.
+// A chain lives inside one asm statement, the only place the code survives.
+
+// a + b mod 2^192.
+__device__ __forceinline__ W3 add_w3(W3 a, W3 b) {
+  W3 r;
+  asm("add.cc.u64 %0, %3, %6;\n\t"
+      "addc.cc.u64 %1, %4, %7;\n\t"
+      "addc.u64 %2, %5, %8;"
+      : "=l"(r.w0), "=l"(r.w1), "=l"(r.w2)
+      : "l"(a.w0), "l"(a.w1), "l"(a.w2), "l"(b.w0), "l"(b.w1), "l"(b.w2));
+  return r;
+}
+
+// y[0..8) += a0 + a1 * 2^64 (a carry rippling through all eight words);
+// returns the carry out of the top word.
+__device__ __forceinline__ u64 add_ripple8(u64 (&y)[8], u64 a0, u64 a1) {
+  u64 c;
+  asm("add.cc.u64 %0, %0, %9;\n\t"
+      "addc.cc.u64 %1, %1, %10;\n\t"
+      "addc.cc.u64 %2, %2, 0;\n\t"
+      "addc.cc.u64 %3, %3, 0;\n\t"
+      "addc.cc.u64 %4, %4, 0;\n\t"
+      "addc.cc.u64 %5, %5, 0;\n\t"
+      "addc.cc.u64 %6, %6, 0;\n\t"
+      "addc.cc.u64 %7, %7, 0;\n\t"
+      "addc.u64 %8, 0, 0;"
+      : "+l"(y[0]), "+l"(y[1]), "+l"(y[2]), "+l"(y[3]), "+l"(y[4]), "+l"(y[5]), "+l"(y[6]), "+l"(y[7]), "=l"(c)
+      : "l"(a0), "l"(a1));
+  return c;
+}
+
 // Garner: x = r0 + p0*u + p0*p1*v with u = (r1-r0)/p0 mod p1 and
 // v = ((r2-r0)/p0 - u)/p1 mod p2; residues in [0,p) after the inverse.
 template <bool CG>
@@ -67,40 +100,23 @@ struct CrtProducerT {
     const u64 t2 = shoup_mul_c<2>(d2, P.inv02, P.inv02s);
     const u64 e2 = t2 >= u ? t2 - u : t2 + p2 - u;
     const u64 v = shoup_mul_c<2>(e2, P.inv12, P.inv12s);
-    // lo = p0*u + x0
-    u64 l0 = p0 * u, l1 = mulhi(p0, u);
-    l0 += x0;
-    l1 += (l0 < x0);
-    // m = p01_lo * v, h = p01_hi * v
-    const u64 m0 = P.p01_lo * v, m1 = mulhi(P.p01_lo, v);
-    const u64 h0 = P.p01_hi * v, h1 = mulhi(P.p01_hi, v);
+    // x0 + p0*u + (p01_lo + p01_hi*2^64)*v as one carry chain
     W3 r;
-    r.w0 = l0 + m0;
-    u64 c = r.w0 < l0;
-    u64 s1 = l1 + m1;
-    u64 c2 = s1 < l1;
-    s1 += h0;
-    c2 += s1 < h0;
-    s1 += c;
-    c2 += s1 < c;
-    r.w1 = s1;
-    r.w2 = h1 + c2;
+    asm("mad.lo.cc.u64 %0, %3, %4, %5;\n\t"
+        "madc.hi.u64 %1, %3, %4, 0;\n\t"
+        "mad.lo.cc.u64 %0, %6, %8, %0;\n\t"
+        "madc.hi.cc.u64 %1, %6, %8, %1;\n\t"
+        "madc.hi.u64 %2, %7, %8, 0;\n\t"
+        "mad.lo.cc.u64 %1, %7, %8, %1;\n\t"
+        "addc.u64 %2, %2, 0;"
+        : "=l"(r.w0), "=l"(r.w1), "=l"(r.w2)
+        : "l"(p0), "l"(u), "l"(x0), "l"(P.p01_lo), "l"(P.p01_hi), "l"(v));
     return r;
   }
 };
 
 typedef CrtProducerT<false> CrtProducer;
 
-__device__ __forceinline__ W3 add_w3(W3 a, W3 b) {
-  W3 r;
-  r.w0 = a.w0 + b.w0;
-  const u64 c0 = r.w0 < a.w0;
-  const u64 t = a.w1 + b.w1;
-  const u64 c1 = t < a.w1;
-  r.w1 = t + c0;
-  r.w2 = a.w2 + b.w2 + c1 + (r.w1 < t);
-  return r;
-}
 
 // A product split into pieces: the longer operand x (nx limbs) cut into P
 // pieces of k limbs (the last one shorter), each multiplied by the shorter
@@ -290,16 +306,10 @@ __device__ __forceinline__ void scan_tile(const Prod& prod, u64 tile, u64 total,
   }
 #pragma unroll
   for (int e = 0; e < E; ++e) {
-    const W3 x = xs[e];
-    const u64 s0 = x.w0 + c0;
-    const u64 cy0 = s0 < c0;
-    u64 s1 = x.w1 + c1;
-    u64 cy1 = s1 < c1;
-    s1 += cy0;
-    cy1 += s1 < cy0;
-    y[e] = s0;
-    c0 = s1;
-    c1 = x.w2 + cy1;
+    const W3 t = add_w3(xs[e], W3{c0, c1, 0});
+    y[e] = t.w0;
+    c0 = t.w1;
+    c1 = t.w2;
   }
   s_h0[tid] = c0;
   s_h1[tid] = c1;
@@ -319,15 +329,9 @@ __device__ __forceinline__ void scan_tile(const Prod& prod, u64 tile, u64 total,
   if (tid == 0 && tile != 0) {
     u64 d0 = 0, d1 = 0;
     for (int e = 0; e < E; ++e) {
-      const W3 x{s_x[e][0], s_x[e][1], s_x[e][2]};
-      const u64 s0 = x.w0 + d0;
-      const u64 cy0 = s0 < d0;
-      u64 s1 = x.w1 + d1;
-      u64 cy1 = s1 < d1;
-      s1 += cy0;
-      cy1 += s1 < cy0;
-      d0 = s1;
-      d1 = x.w2 + cy1;
+      const W3 t = add_w3(W3{s_x[e][0], s_x[e][1], s_x[e][2]}, W3{d0, d1, 0});
+      d0 = t.w1;
+      d1 = t.w2;
     }
     hp0 = d0;
     hp1 = d1;
@@ -337,29 +341,13 @@ __device__ __forceinline__ void scan_tile(const Prod& prod, u64 tile, u64 total,
     hp0 = s_h0[tid - 1];
     hp1 = s_h1[tid - 1];
   }
-  // u_t = lo_t + H_{t-1}
-  {
-    u64 t = y[0] + hp0;
-    u64 cy = t < hp0;
-    y[0] = t;
-    u64 t1 = y[1] + hp1;
-    u64 cy1 = t1 < hp1;
-    t1 += cy;
-    cy1 += t1 < cy;
-    y[1] = t1;
-    u64 c = cy1;
+  // u_t = lo_t + H_{t-1}; the carry out is the generate bit
+  static_assert(E == 8, "the carry chains take eight limbs a thread");
+  const u32 g = (u32)add_ripple8(y, hp0, hp1);
+  u64 all = y[0];
 #pragma unroll
-    for (int e = 2; e < E; ++e) {
-      y[e] += c;
-      c = c && y[e] == 0;
-    }
-    hp0 = c;  // generate bit
-  }
-  const u32 g = (u32)hp0;
-  u32 pr = 1;
-#pragma unroll
-  for (int e = 0; e < E; ++e) pr &= (y[e] == ~0ull);
-  pr &= !g;
+  for (int e = 1; e < E; ++e) all &= y[e];
+  const u32 pr = (all == ~0ull) & !g;
 
   const u32 G = __ballot_sync(0xffffffffu, g);
   const u32 GP = __ballot_sync(0xffffffffu, g | pr);
@@ -416,12 +404,7 @@ __device__ __forceinline__ void scan_tile(const Prod& prod, u64 tile, u64 total,
   for (int w = 0; w < warp; ++w) wc = s_wg[w] | (s_wp[w] & wc);
   const u64 sum = (u64)G + GP + wc;
   const u32 cin_bits = (u32)sum ^ G ^ GP;
-  u32 c = (cin_bits >> lane) & 1;
-#pragma unroll
-  for (int e = 0; e < E; ++e) {
-    y[e] += c;
-    c = c && y[e] == 0;
-  }
+  add_ripple8(y, (cin_bits >> lane) & 1, 0);  // its carry out is the next thread's carry-in, counted above
 #pragma unroll
   for (int e = 0; e < E; ++e) {
     const u64 k = k0 + e;
