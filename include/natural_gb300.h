@@ -296,7 +296,7 @@ nn_status nn_e_dec_host(nn_context* ctx, uint64_t terms, uint64_t digits, char**
  * evaluated level by level, each level's products as one GPU batch; the
  * series trees' bottom subtrees, whose values stay below about host_below
  * limbs (256 is a good choice), run whole on host threads.  The decimal split
- * runs its levels while the split powers have at least host_below / 2 limbs;
+ * runs its levels while the split powers have at least host_below limbs;
  * the nodes left become digits on the device (one thread a node peels off
  * 18-digit groups, natural.h:566-573 and 994-1011) and come back in one copy.
  * terms must be a power of two (the trees are then perfect).  timing (8

@@ -204,6 +204,22 @@ __global__ void wait_probe_kernel(const u32* flag, u32* err, int limit) {
   if (threadIdx.x == 0 && wait_flag(flag, limit) == 0) atomicExch(err, 1u);
 }
 
+// Base-case products of at most kColumnSumPositions positions go in two
+// launches: their column sums, one thread a position (a warp reads one limb
+// of a and 32 consecutive limbs of b at a time), into the scan's sums; then
+// the carry scan over them.  The one-launch scan gives each thread eight
+// positions, so a product of a few hundred limbs has one CTA of threads that
+// each add eight columns in turn (measured: 383 x 383 limbs, 137 us).
+constexpr u64 kColumnSumPositions = 1 << 20;  // 24 MiB of sums
+__global__ void __launch_bounds__(256) column_sums_kernel(ColumnProducer prod, u64 total, u64* sums) {
+  const u64 k = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= total) return;
+  const W3 r = prod(k);
+  sums[k] = r.w0;
+  sums[total + k] = r.w1;
+  sums[2 * total + k] = r.w2;
+}
+
 // Tiles [tile_begin, tile_end) of the scan (all of them by default).  The
 // ranges of one scan go in order on one stream (each range's carry-in comes
 // from the range before: through the status words of the lookback, or the
@@ -272,6 +288,7 @@ cudaError_t scan_reserve(Scan& sc, u64 tiles) {
 void scan_free(Scan& sc) {
   if (sc.flags) cudaFree(sc.flags);
   if (sc.counter) cudaFree(sc.counter);
+  if (sc.sums) cudaFree(sc.sums);
   sc = Scan{};
 }
 
@@ -310,7 +327,23 @@ cudaError_t ntt_save_chunks(const u64* res, int s, u64* out, u64 size, Scan& sc,
 cudaError_t school_mul(const u64* a, u64 na, const u64* b, u64 nb, u64* out, Scan& sc, cudaStream_t st) {
   cudaError_t e = scan_reserve(sc, 1);
   if (e != cudaSuccess) return e;
-  return run_scan(ColumnProducer{a, na, b, nb}, na + nb, out, na + nb, sc, st, "school_column_scan");
+  const u64 total = na + nb;
+  if (total > kColumnSumPositions)
+    return run_scan(ColumnProducer{a, na, b, nb}, total, out, total, sc, st, "school_column_scan");
+  if (sc.sums_cap < total) {
+    if (sc.sums) cudaFree(sc.sums);
+    sc.sums = nullptr;
+    sc.sums_cap = 0;
+    e = cudaMalloc((void**)&sc.sums, 3 * kColumnSumPositions * sizeof(u64));
+    if (e != cudaSuccess) return e;
+    sc.sums_cap = kColumnSumPositions;
+  }
+  launch_begin("school_column_sums", st);
+  column_sums_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(ColumnProducer{a, na, b, nb}, total, sc.sums);
+  launch_end(st);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return run_scan(SumsProducer{sc.sums, total}, total, out, total, sc, st, "school_column_scan");
 }
 
 cudaError_t add_shifted(const u64* x, u64 nx, const u64* y, u64 ny, u64 shift, u64* out, u64 n, Scan& sc,

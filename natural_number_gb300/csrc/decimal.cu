@@ -66,22 +66,41 @@ __device__ __forceinline__ void put18(char* o, u64 x) {
   for (int t = 0; t < 9; ++t) o2[t] = (unsigned short)(d[2 * t] | (d[2 * t + 1] << 8));
 }
 
+// Limbs a thread loads at once while it divides the previous batch: the
+// division chain runs from the top limb down, so the loads of the next
+// kChunk limbs are independent of it and their latency overlaps the work.
+constexpr int kChunk = 8;
+
 __global__ void __launch_bounds__(128) dec_groups_kernel(u64* w, const u32* len, u64 n, u32 groups, u64 v, char* out) {
   const u64 k = (u64)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   u32 m = len[k];
   char* o = out + k * (u64)groups * 18;
+  // limb j of this node, or 0 below limb 0
+  auto load = [&](long long j) -> u64 { return j >= 0 ? w[(u64)j * n + k] : 0; };
   for (u32 g = groups; g-- > 0;) {
     // node := floor(node / 10^18), remainder r: the dividend is shifted left
     // by kNorm bits on the fly (u1 = 16 r + top bits of the limb, u1 < 16 * 10^18)
     u64 rn = 0;
     const u32 top = m;
-    for (u32 j = top; j-- > 0;) {
-      u64* p = w + (u64)j * n + k;
-      const u64 a = *p;
-      const u64 q = div_2by1(rn | (a >> (64 - kNorm)), a << kNorm, kGroupNorm, v, rn);
-      *p = q;
-      if (j == top - 1 && q == 0) --m;  // the value loses at most one limb per division (10^18 < 2^64)
+    u64 cur[kChunk], nxt[kChunk];
+#pragma unroll
+    for (int t = 0; t < kChunk; ++t) cur[t] = load((long long)top - 1 - t);
+    for (long long j0 = (long long)top - 1; j0 >= 0; j0 -= kChunk) {
+#pragma unroll
+      for (int t = 0; t < kChunk; ++t) nxt[t] = load(j0 - kChunk - t);
+#pragma unroll
+      for (int t = 0; t < kChunk; ++t) {
+        const long long j = j0 - t;
+        if (j >= 0) {
+          const u64 a = cur[t];
+          const u64 q = div_2by1(rn | (a >> (64 - kNorm)), a << kNorm, kGroupNorm, v, rn);
+          w[(u64)j * n + k] = q;
+          if (j == (long long)top - 1 && q == 0) --m;  // at most one limb lost a division (10^18 < 2^64)
+        }
+      }
+#pragma unroll
+      for (int t = 0; t < kChunk; ++t) cur[t] = nxt[t];
     }
     put18(o + (u64)g * 18, rn >> kNorm);
   }

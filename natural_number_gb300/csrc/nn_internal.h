@@ -55,6 +55,8 @@ struct Scan {
   u32* chain = nullptr;  // carry between consecutive tile ranges of one scan
   u64* side = nullptr;   // limbs of the scan beyond the output (the carry words)
   u64 max_tiles = 0;
+  u64* sums = nullptr;   // column sums of base-case products, three words a position
+  u64 sums_cap = 0;      // positions they have room for
 };
 constexpr int kScanThreads = 256;
 constexpr int kScanE = 8;  // limbs per thread

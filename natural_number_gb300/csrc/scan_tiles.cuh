@@ -189,6 +189,23 @@ struct ColumnProducer {
   }
 };
 
+// Three-word values stored as three arrays (word i of position k at
+// s[i * total + k]): the column sums of a base-case product, computed before
+// the scan by one thread a position.
+struct SumsProducer {
+  static constexpr bool kBulk = true;
+  const u64* s;
+  u64 total;
+  __device__ __forceinline__ W3 operator()(u64 k) const {
+    if (k >= total) return W3{0, 0, 0};
+    return W3{s[k], s[total + k], s[2 * total + k]};
+  }
+  __device__ __forceinline__ void bulk(u64 k0, W3 (&x)[kScanE]) const {
+#pragma unroll
+    for (int e = 0; e < kScanE; ++e) x[e] = (*this)(k0 + e);
+  }
+};
+
 // x[k] + y[k - shift] (two words).
 struct AddProducer {
   static constexpr bool kBulk = false;

@@ -590,10 +590,11 @@ char* to_dec_levels(nn_context* c, const natural& x, u64 host_below, Staging& st
   std::vector<Node> lv;
   lv.push_back(Node{x, true});
   int i = top;
-  // GPU levels down to half the tree's threshold: below it a host subtree's
-  // O(n^2) schoolbook splits cost more than another batched level (measured
-  // on GB300 for pi and e to 10^8 digits: 128 limbs at the default 256)
-  const u64 dec_below = std::max<u64>(host_below / 2, 16);
+  // Split levels while the split powers have at least host_below limbs: the
+  // device leaves below cost less than another batched level down to about
+  // there (measured on GB300, a 5 Mi-limb value to 10^8 digits: 0.192 s with
+  // levels down to 128 limbs, 0.167 s to 256, 0.181 s to 512)
+  const u64 dec_below = std::max<u64>(host_below, 16);
   for (; i >= 1 && std::min(D[i].nb, D[i].nr) >= dec_below; --i) {
     const natural& base = C.base[i];
     const natural& base_r = C.base_r[i];
