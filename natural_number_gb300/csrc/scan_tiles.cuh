@@ -422,6 +422,11 @@ __device__ __forceinline__ void scan_tile(const Prod& prod, u64 tile, u64 total,
   const u64 sum = (u64)G + GP + wc;
   const u32 cin_bits = (u32)sum ^ G ^ GP;
   add_ripple8(y, (cin_bits >> lane) & 1, 0);  // its carry out is the next thread's carry-in, counted above
+  if (k0 + E <= out_limit && k0 + E <= total && !(reinterpret_cast<uintptr_t>(out) & 15)) {
+#pragma unroll
+    for (int e = 0; e < E; e += 2) *reinterpret_cast<ulonglong2*>(out + k0 + e) = make_ulonglong2(y[e], y[e + 1]);
+    return;
+  }
 #pragma unroll
   for (int e = 0; e < E; ++e) {
     const u64 k = k0 + e;
