@@ -553,7 +553,7 @@ def main() -> None:
         ha = torch.from_numpy(st["a"]).pin_memory().numpy()
         hb = torch.from_numpy(st["b"]).pin_memory().numpy()
         ho = torch.empty(2 * n, dtype=torch.uint64).pin_memory().numpy()
-        for _ in range(2):
+        for _ in range(max(2, args.warmup)):
             ctx.mul(ha, hb, out=ho)
         replicas.barrier(dist)
         step_ms = []
@@ -570,7 +570,7 @@ def main() -> None:
                 "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 16 * n,
                 "api": "nn_mul_host (page-locked host operands in, product out, every step)",
                 "step_ms_median": statistics.median(step_ms), "step_ms_min": min(step_ms),
-                "step_ms_max": max(step_ms)}
+                "step_ms_max": max(step_ms), "step_ms": [round(x, 1) for x in step_ms]}
 
     if not args.no_e2e:
         r = legs.run("e2e", 180, e2e, core=True)
