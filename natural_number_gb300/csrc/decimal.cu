@@ -5,18 +5,29 @@
 // natural.h:953-967; the last split is div_base by 10^18, natural.h:566-573)
 // and prints each leaf as 18 zero-padded digits (the first one unpadded).
 // The decimal digits of a value are unique, so a node of the tree at any
-// level has exactly one digit string of its width; here one thread takes one
+// level has exactly one digit string of its width; here one warp takes one
 // node and peels off its 18-digit groups from the low end by repeated exact
 // division by 10^18, which is div_base's step applied 2^(i+1) times.
 //
-// Layout: the nodes' limbs are limb-major, w[j * n + k] = limb j of node k,
-// so that the threads of a warp, each on its own node, touch consecutive
-// words.  Node k's digits go to out[k * width, (k + 1) * width), width = 18 *
-// groups, most significant group first.  Every division is done in place.
+// A division's remainder chain runs from the top limb down, one limb after
+// the other.  The warp splits it: lane l takes a segment of the node's limbs
+// and reduces it to the map r -> (r * 2^(64 len) + segment) mod 10^18 (the
+// remainder its segment leaves for a remainder r coming in from above); a
+// scan over the lanes composes these maps from the top, so every lane knows
+// the remainder entering its segment, and the lanes then form their
+// quotient limbs at once.  A division costs two passes over a segment plus
+// five compositions instead of one pass over the whole node.
+//
+// Layout: node k's limbs at w[k * stride ...), copied into shared memory,
+// divided there; its digits go to out[k * width, (k + 1) * width), width =
+// 18 * groups, most significant group first.
 #include <cuda_runtime.h>
 
 #include "nn_device.cuh"
 #include "nn_internal.h"
+
+#include <algorithm>
+#include <atomic>
 
 namespace nn {
 
@@ -66,55 +77,107 @@ __device__ __forceinline__ void put18(char* o, u64 x) {
   for (int t = 0; t < 9; ++t) o2[t] = (unsigned short)(d[2 * t] | (d[2 * t + 1] << 8));
 }
 
-// Limbs a thread loads at once while it divides the previous batch: the
-// division chain runs from the top limb down, so the loads of the next
-// kChunk limbs are independent of it and their latency overlaps the work.
-constexpr int kChunk = 8;
+// (a * b) mod 10^18 for a, b < 10^18: the product's high word is below the
+// divisor, as the two-by-one division wants after the shift by kNorm.
+__device__ __forceinline__ u64 mulmod_group(u64 a, u64 b, u64 v) {
+  const u64 lo = a * b, hi = __umul64hi(a, b);
+  u64 r;
+  div_2by1((hi << kNorm) | (lo >> (64 - kNorm)), lo << kNorm, kGroupNorm, v, r);
+  return r >> kNorm;
+}
 
-__global__ void __launch_bounds__(128) dec_groups_kernel(u64* w, const u32* len, u64 n, u32 groups, u64 v, char* out) {
-  const u64 k = (u64)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
+// 2^(64 j) mod 10^18 for the segment lengths j <= kMaxSegment.
+constexpr int kMaxSegment = 256;
+constexpr int kMaxDevices = 64;
+__constant__ u64 c_limb_pow[kMaxSegment + 1];
+
+// One warp a node; `per_cta` warps a CTA, each with `stride` limbs of shared
+// memory.  A division pass over the current m limbs: segments of
+// ceil(m / 32) limbs, lane l holding limbs [l * seg, (l + 1) * seg).
+__global__ void __launch_bounds__(128) dec_groups_kernel(const u64* __restrict__ w, u64 stride,
+                                                         const u32* __restrict__ len, u64 n, u32 groups, u64 v,
+                                                         char* out) {
+  extern __shared__ u64 node_sm[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const u64 k = (u64)blockIdx.x * (blockDim.x >> 5) + warp;
+  if (k >= n) return;  // a whole warp leaves together
+  u64* a = node_sm + (u64)warp * stride;
   u32 m = len[k];
+  for (u32 j = lane; j < m; j += 32) a[j] = w[k * stride + j];
+  __syncwarp();
   char* o = out + k * (u64)groups * 18;
-  // limb j of this node, or 0 below limb 0
-  auto load = [&](long long j) -> u64 { return j >= 0 ? w[(u64)j * n + k] : 0; };
   for (u32 g = groups; g-- > 0;) {
-    // node := floor(node / 10^18), remainder r: the dividend is shifted left
-    // by kNorm bits on the fly (u1 = 16 r + top bits of the limb, u1 < 16 * 10^18)
+    const u32 seg = (m + 31) / 32;  // at most kMaxSegment: m is below 32 * kMaxSegment
+    const u32 lo = min(lane * seg, m), hi = min(lo + seg, m);
+    // this lane's map r -> A r + B: B = its segment mod 10^18, A = 2^(64 len) mod 10^18
     u64 rn = 0;
-    const u32 top = m;
-    u64 cur[kChunk], nxt[kChunk];
-#pragma unroll
-    for (int t = 0; t < kChunk; ++t) cur[t] = load((long long)top - 1 - t);
-    for (long long j0 = (long long)top - 1; j0 >= 0; j0 -= kChunk) {
-#pragma unroll
-      for (int t = 0; t < kChunk; ++t) nxt[t] = load(j0 - kChunk - t);
-#pragma unroll
-      for (int t = 0; t < kChunk; ++t) {
-        const long long j = j0 - t;
-        if (j >= 0) {
-          const u64 a = cur[t];
-          const u64 q = div_2by1(rn | (a >> (64 - kNorm)), a << kNorm, kGroupNorm, v, rn);
-          w[(u64)j * n + k] = q;
-          if (j == (long long)top - 1 && q == 0) --m;  // at most one limb lost a division (10^18 < 2^64)
-        }
-      }
-#pragma unroll
-      for (int t = 0; t < kChunk; ++t) cur[t] = nxt[t];
+    for (u32 j = hi; j-- > lo;) {
+      const u64 x = a[j];
+      div_2by1(rn | (x >> (64 - kNorm)), x << kNorm, kGroupNorm, v, rn);
     }
-    put18(o + (u64)g * 18, rn >> kNorm);
+    u64 A = c_limb_pow[hi - lo], B = rn >> kNorm;
+    // compose from the top: lane l ends with the map of segments l .. 31
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const u64 A2 = __shfl_down_sync(0xffffffffu, A, d), B2 = __shfl_down_sync(0xffffffffu, B, d);
+      if (lane + d < 32) {
+        B = mulmod_group(A, B2, v) + B;
+        if (B >= kGroup) B -= kGroup;
+        A = mulmod_group(A, A2, v);
+      }
+    }
+    const u64 group = __shfl_sync(0xffffffffu, B, 0);  // the remainder of the whole node
+    u64 rin = __shfl_down_sync(0xffffffffu, B, 1);
+    if (lane == 31) rin = 0;
+    // the quotient limbs, every segment at once
+    rn = rin << kNorm;
+    u64 top_q = 1;
+    for (u32 j = hi; j-- > lo;) {
+      const u64 x = a[j];
+      const u64 q = div_2by1(rn | (x >> (64 - kNorm)), x << kNorm, kGroupNorm, v, rn);
+      a[j] = q;
+      if (j == m - 1) top_q = q;
+    }
+    // the value loses at most one limb a division (10^18 < 2^64)
+    const bool lost = __any_sync(0xffffffffu, m > 0 && hi == m && hi > lo && top_q == 0);
+    __syncwarp();
+    if (lost) --m;
+    if (lane == 0) put18(o + (u64)g * 18, group);
   }
 }
 
 }  // namespace
 
-cudaError_t dec_groups(u64* w, const u32* len, u64 n, u32 groups, char* out, cudaStream_t st) {
+cudaError_t dec_groups(const u64* w, u64 stride, const u32* len, u64 n, u32 groups, char* out, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
+  if (stride > (u64)32 * kMaxSegment || stride % 2) return cudaErrorInvalidValue;
+  // 2^(64 j) mod 10^18 into the constant bank, once per device (each device
+  // has its own copy of c_limb_pow)
+  static std::atomic<bool> powers[kMaxDevices];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  if (!powers[dev].load()) {
+    u64 t[kMaxSegment + 1];
+    unsigned __int128 x = 1;
+    for (int j = 0; j <= kMaxSegment; ++j, x = (x << 64) % kGroup) t[j] = (u64)x;
+    e = cudaMemcpyToSymbol(c_limb_pow, t, sizeof t);
+    if (e != cudaSuccess) return e;
+    powers[dev].store(true);
+  }
   const unsigned __int128 all = ~(unsigned __int128)0;
   const u64 v = (u64)(all / kGroupNorm);  // floor((2^128-1)/d) - 2^64: the 2^64 bit drops in the cast
-  const unsigned threads = 128;
+  // warps a CTA: as many nodes as 48 KiB of shared memory holds, at most four
+  const unsigned per_cta = (unsigned)std::max<u64>(1, std::min<u64>(4, (48 * 1024) / (8 * stride)));
+  const size_t smem = (size_t)per_cta * stride * 8;
+  if (smem > 48 * 1024) {
+    e = cudaFuncSetAttribute(dec_groups_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
   launch_begin("dec_groups", st);
-  dec_groups_kernel<<<(unsigned)((n + threads - 1) / threads), threads, 0, st>>>(w, len, n, groups, v, out);
+  dec_groups_kernel<<<(unsigned)((n + per_cta - 1) / per_cta), 32 * per_cta, smem, st>>>(w, stride, len, n, groups, v,
+                                                                                          out);
   launch_end(st);
   return cudaGetLastError();
 }

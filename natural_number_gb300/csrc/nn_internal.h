@@ -149,11 +149,11 @@ cudaError_t shr_bits(u64* out, const u64* in, u64 n, unsigned cl, cudaStream_t s
 // most `limit` polls); it gives up and sets sc.err, which the host reads.
 cudaError_t wait_probe(Scan& sc, int limit, cudaStream_t st);
 
-// Decimal digits of n short naturals at once (decimal.cu): w holds their
-// limbs limb-major (w[j * n + k] = limb j of node k, len[k] limbs, divided in
-// place); node k < 10^(18 * groups) goes to out[k * 18 * groups ...) as
-// 18 * groups zero-padded digits, most significant first.
-cudaError_t dec_groups(u64* w, const u32* len, u64 n, u32 groups, char* out, cudaStream_t st);
+// Decimal digits of n short naturals at once (decimal.cu): node k's len[k]
+// limbs at w[k * stride ...) (stride even, at most 8192); node k < 10^(18 *
+// groups) goes to out[k * 18 * groups ...) as 18 * groups zero-padded
+// digits, most significant first.
+cudaError_t dec_groups(const u64* w, u64 stride, const u32* len, u64 n, u32 groups, char* out, cudaStream_t st);
 
 // Launch accounting (profile.cpp): every launch site brackets its kernel.
 void launch_begin(const char* name, cudaStream_t st);

@@ -594,7 +594,8 @@ char* to_dec_levels(nn_context* c, const natural& x, u64 host_below, Staging& st
   // device leaves below cost less than another batched level down to about
   // there (measured on GB300, a 5 Mi-limb value to 10^8 digits: 0.192 s with
   // levels down to 128 limbs, 0.167 s to 256, 0.181 s to 512)
-  const u64 dec_below = std::max<u64>(host_below, 16);
+  // (at most 4000 limbs: the device leaves then stay within 8192 limbs a node)
+  const u64 dec_below = std::min<u64>(std::max<u64>(host_below, 16), 4000);
   for (; i >= 1 && std::min(D[i].nb, D[i].nr) >= dec_below; --i) {
     const natural& base = C.base[i];
     const natural& base_r = C.base_r[i];
@@ -638,32 +639,39 @@ char* to_dec_levels(nn_context* c, const natural& x, u64 host_below, Staging& st
     lv.swap(next);
   }
   // The nodes left, each below base[i]^2 = 10^(18 * 2^(i+1)), on the device:
-  // limb-major in one upload, 2^(i+1) groups of 18 digits a node written in
+  // node-major in one upload, 2^(i+1) groups of 18 digits a node written in
   // place of the tree's leaves (natural.h:994-1011); node 0, the first, is
   // written at the same width and loses its leading zeros on the way back.
   const auto t0 = Clock::now();
   const u64 n = lv.size();
   const u32 groups = 2u << i;
   const u64 width = 18ull * groups;
-  u64 maxlen = 0;
+  u64 maxlen = 2;
   for (const Node& nd : lv) maxlen = std::max(maxlen, span_len(nd.v));
-  const u64 words = maxlen * n + (n + 1) / 2;  // limbs, then the u32 lengths
+  const u64 stride = (maxlen + 1) & ~1ull;
+  const u64 words = stride * n + (n + 1) / 2;  // limbs, then the u32 lengths
   u64* hw = stg.in.get(words);
-  u32* hlen = reinterpret_cast<u32*>(hw + maxlen * n);
-  constexpr u64 kBlock = 64;  // nodes a task transposes: 512-byte runs of each limb row
-  parallel_for((n + kBlock - 1) / kBlock, 1, [&](u64 blk) {
-    const u64 k0 = blk * kBlock, k1 = std::min(n, k0 + kBlock);
-    for (u64 k = k0; k < k1; ++k) hlen[k] = (u32)span_len(lv[k].v);
-    for (u64 j = 0; j < maxlen; ++j)
-      for (u64 k = k0; k < k1; ++k) hw[j * n + k] = j < hlen[k] ? lv[k].v.data[j] : 0;
+  u32* hlen = reinterpret_cast<u32*>(hw + stride * n);
+  parallel_for(n, 64, [&](u64 k) {
+    const u64 l = span_len(lv[k].v);
+    hlen[k] = (u32)l;
+    std::memcpy(hw + k * stride, lv[k].v.data, 8 * l);
   });
   cudaStream_t st = (cudaStream_t)nn_context_stream(c);
-  u64* dw = nullptr;
-  char* dout = nullptr;
-  check_cuda(cudaMallocAsync((void**)&dw, 8 * words, st), "decimal nodes");
-  check_cuda(cudaMallocAsync((void**)&dout, n * width, st), "decimal digits");
+  struct AsyncBuf {  // device buffer freed on the stream however the scope is left
+    cudaStream_t st;
+    void* p = nullptr;
+    ~AsyncBuf() {
+      if (p) cudaFreeAsync(p, st);
+    }
+  } bw{st}, bo{st};
+  check_cuda(cudaMallocAsync(&bw.p, 8 * words, st), "decimal nodes");
+  check_cuda(cudaMallocAsync(&bo.p, n * width, st), "decimal digits");
+  u64* dw = static_cast<u64*>(bw.p);
+  char* dout = static_cast<char*>(bo.p);
   check_cuda(cudaMemcpyAsync(dw, hw, 8 * words, cudaMemcpyHostToDevice, st), "upload");
-  check_cuda(nn::dec_groups(dw, reinterpret_cast<const u32*>(dw + maxlen * n), n, groups, dout, st), "decimal kernel");
+  check_cuda(nn::dec_groups(dw, stride, reinterpret_cast<const u32*>(dw + stride * n), n, groups, dout, st),
+             "decimal kernel");
   std::string head(width, '0');
   check_cuda(cudaMemcpyAsync(head.data(), dout, width, cudaMemcpyDeviceToHost, st), "download");
   check_cuda(cudaStreamSynchronize(st), "decimal digits");
@@ -671,15 +679,9 @@ char* to_dec_levels(nn_context* c, const natural& x, u64 host_below, Staging& st
   while (off + 1 < width && head[off] == '0') ++off;
   const u64 total = n * width - off;
   char* out = static_cast<char*>(std::malloc(total + 1));
-  if (!out) {
-    cudaFreeAsync(dw, st);
-    cudaFreeAsync(dout, st);
-    throw std::bad_alloc();
-  }
+  if (!out) throw std::bad_alloc();
   cudaError_t e = cudaMemcpyAsync(out, dout + off, total, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  cudaFreeAsync(dw, st);
-  cudaFreeAsync(dout, st);
   if (e != cudaSuccess) {
     std::free(out);
     check_cuda(e, "download");
