@@ -205,19 +205,40 @@ __global__ void wait_probe_kernel(const u32* flag, u32* err, int limit) {
 }
 
 // Base-case products of at most kColumnSumPositions positions go in two
-// launches: their column sums, one thread a position (a warp reads one limb
-// of a and 32 consecutive limbs of b at a time), into the scan's sums; then
-// the carry scan over them.  The one-launch scan gives each thread eight
-// positions, so a product of a few hundred limbs has one CTA of threads that
-// each add eight columns in turn (measured: 383 x 383 limbs, 137 us).
+// launches: their column sums into the scan's sums, then the carry scan over
+// them.  A column sum is split over kSumLanes threads (thread j of a column
+// takes every kSumLanes-th term from its own start, so the threads of a
+// column read consecutive limbs of a and of b) and the partial three-word
+// sums meet in three shuffle steps.  The one-launch scan gives each thread
+// eight whole columns, so a product of a few hundred limbs had one CTA of
+// threads that each add eight columns in turn (measured: 383 x 383 limbs,
+// 137 us); one thread a column took 27 us.
 constexpr u64 kColumnSumPositions = 1 << 20;  // 24 MiB of sums
+constexpr int kSumLanes = 8;
 __global__ void __launch_bounds__(256) column_sums_kernel(ColumnProducer prod, u64 total, u64* sums) {
-  const u64 k = (u64)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= total) return;
-  const W3 r = prod(k);
-  sums[k] = r.w0;
-  sums[total + k] = r.w1;
-  sums[2 * total + k] = r.w2;
+  const u64 t = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+  const u64 k = t / kSumLanes;
+  const u32 j = (u32)(t % kSumLanes);
+  W3 r{0, 0, 0};
+  if (k < total && k + 1 < prod.na + prod.nb) {
+    const u64 lo = k >= prod.nb ? k - prod.nb + 1 : 0;
+    const u64 hi = k < prod.na - 1 ? k : prod.na - 1;
+    for (u64 i = lo + j; i <= hi; i += kSumLanes) {
+      const u64 x = prod.a[i], y = prod.b[k - i];
+      r = add_w3(r, W3{x * y, mulhi(x, y), 0});
+    }
+  }
+#pragma unroll
+  for (int d = kSumLanes / 2; d >= 1; d >>= 1) {  // every lane of the warp takes part
+    const W3 o{__shfl_down_sync(0xffffffffu, r.w0, d, kSumLanes), __shfl_down_sync(0xffffffffu, r.w1, d, kSumLanes),
+               __shfl_down_sync(0xffffffffu, r.w2, d, kSumLanes)};
+    r = add_w3(r, o);
+  }
+  if (j == 0 && k < total) {
+    sums[k] = r.w0;
+    sums[total + k] = r.w1;
+    sums[2 * total + k] = r.w2;
+  }
 }
 
 // Tiles [tile_begin, tile_end) of the scan (all of them by default).  The
@@ -339,7 +360,8 @@ cudaError_t school_mul(const u64* a, u64 na, const u64* b, u64 nb, u64* out, Sca
     sc.sums_cap = kColumnSumPositions;
   }
   launch_begin("school_column_sums", st);
-  column_sums_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(ColumnProducer{a, na, b, nb}, total, sc.sums);
+  column_sums_kernel<<<(unsigned)((total * kSumLanes + 255) / 256), 256, 0, st>>>(ColumnProducer{a, na, b, nb}, total,
+                                                                                 sc.sums);
   launch_end(st);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
