@@ -213,7 +213,7 @@ __global__ void wait_probe_kernel(const u32* flag, u32* err, int limit) {
 // eight whole columns, so a product of a few hundred limbs had one CTA of
 // threads that each add eight columns in turn (measured: 383 x 383 limbs,
 // 137 us); one thread a column took 27 us.
-constexpr u64 kColumnSumPositions = 1 << 20;  // 24 MiB of sums
+constexpr u64 kColumnSumPositions = 1 << 20;  // at most 24 MiB of sums
 constexpr int kSumLanes = 8;
 __global__ void __launch_bounds__(256) column_sums_kernel(ColumnProducer prod, u64 total, u64* sums) {
   const u64 t = (u64)blockIdx.x * blockDim.x + threadIdx.x;
@@ -351,13 +351,15 @@ cudaError_t school_mul(const u64* a, u64 na, const u64* b, u64 nb, u64* out, Sca
   const u64 total = na + nb;
   if (total > kColumnSumPositions)
     return run_scan(ColumnProducer{a, na, b, nb}, total, out, total, sc, st, "school_column_scan");
-  if (sc.sums_cap < total) {
+  if (sc.sums_cap < total) {  // grow-only, by doubling from 4096 positions (96 KiB)
+    u64 cap = std::max<u64>(sc.sums_cap, 4096);
+    while (cap < total) cap *= 2;
     if (sc.sums) cudaFree(sc.sums);
     sc.sums = nullptr;
     sc.sums_cap = 0;
-    e = cudaMalloc((void**)&sc.sums, 3 * kColumnSumPositions * sizeof(u64));
+    e = cudaMalloc((void**)&sc.sums, 3 * cap * sizeof(u64));
     if (e != cudaSuccess) return e;
-    sc.sums_cap = kColumnSumPositions;
+    sc.sums_cap = cap;
   }
   launch_begin("school_column_sums", st);
   column_sums_kernel<<<(unsigned)((total * kSumLanes + 255) / 256), 256, 0, st>>>(ColumnProducer{a, na, b, nb}, total,
