@@ -214,3 +214,32 @@ def test_multi_step_scan_vs_oracle(ctx, oracle):
     ctx.mul_device(out, to_dev(a), to_dev(b))
     assert np.array_equal(to_host(out), want)
     assert np.array_equal(ctx.mul(a, b), want)
+
+
+@pytest.mark.parametrize("na,nb", [(300, 200), (383, 383), (5000, 3001), (1 << 16, 1 << 16), (200000, 70001)])
+def test_products_on_8_byte_aligned_buffers(ctx, oracle, na, nb):
+    """Operands and products one limb into their buffers (8-byte, not 16-byte,
+    aligned): the first pass's limb loads take their scalar path and the
+    carry scan its scalar stores, and the results equal the oracle's."""
+    a, b = limbs(8000 + na, na), limbs(9000 + nb, nb)
+    da, db = empty_dev(na + 1), empty_dev(nb + 1)
+    da[1:] = to_dev(a)
+    db[1:] = to_dev(b)
+    out = empty_dev(na + nb + 1)
+    ctx.mul_device(out[1:], da[1:], db[1:])
+    assert np.array_equal(normalize(to_host(out)[1:]), oracle.mul(a, b))
+    out2 = empty_dev(2 * na + 1)
+    ctx.sqr_device(out2[1:], da[1:])
+    assert np.array_equal(normalize(to_host(out2)[1:]), oracle.sqr(a))
+
+
+def test_wrap_mode_on_8_byte_aligned_buffers(ctx, oracle):
+    """The wrap-mode pipeline with operands and output one limb into their
+    buffers, against the oracle."""
+    s, size = 14, (1 << 14) + 9
+    a, b = limbs(77, 12000), limbs(78, 9000)
+    da, db, out = empty_dev(12001), empty_dev(9001), empty_dev((1 << s) + 1)
+    da[1:] = to_dev(a)
+    db[1:] = to_dev(b)
+    w = ctx.ntt_mul_device(out[1:], da[1:], db[1:], s, size)
+    assert np.array_equal(to_host(out)[1:1 + w], oracle.ntt_mul_raw(a, b, s, size))
