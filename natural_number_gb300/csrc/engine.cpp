@@ -39,7 +39,7 @@ struct nn_context {
   // host-pointer calls: the second operand's copy runs on `copy` while the
   // first operand is transformed
   cudaStream_t copy = nullptr;
-  cudaEvent_t ev_first = nullptr, ev_second = nullptr, ev_chunk = nullptr;
+  cudaEvent_t ev_first = nullptr, ev_second = nullptr, ev_chunk = nullptr, ev_in = nullptr;
   u64 budget = 0;
   u64 held = 0;  // bytes of live allocations made through the context
   nn::Tables tables;
@@ -260,6 +260,54 @@ nn_status ntt_product(nn_context* c, u64* d_out, const u64* a, u64 na, const u64
     if (st == NN_OK) st = pointwise(c, &xb, &xa, &xb);
     if (st == NN_OK) st = inverse_save(c, &xb, d_out, size, written);
   }
+  dev_free(c, xa.res, xa.words);
+  dev_free(c, xb.res, xb.words);
+  return st;
+}
+
+// Balanced NTT product of host operands (ha: na limbs, hb: nb limbs, na >=
+// nb) into d_out and h_out.  a's copy to da goes a range of columns at a time
+// (kInChunks ranges: a 2-D copy of the range in every full row of the first
+// pass, plus its part of a last, partial row) on the copy stream, and the
+// first forward pass runs each range's tiles as soon as it has arrived, so
+// the copy overlaps that pass; b's copy follows on the same stream while a's
+// other passes run.  *used is false, and nothing is done, when the plan's
+// first pass cannot run by ranges.
+constexpr int kInChunks = 8;
+nn_status ntt_product_from_host(nn_context* c, u64* d_out, u64* da, const u64* ha, u64 na, u64* db, const u64* hb,
+                                u64 nb, int s, u64* h_out, bool* used) {
+  *used = false;
+  const std::vector<nn::Pass> plan = c->passes(s);
+  u64 tiles = 0;
+  if (plan.size() < 2 || !nn::ntt_first_pass_tiles(s, plan[0], &tiles)) return NN_OK;
+  *used = true;
+  NN_CK(c, nn::tables_ensure(c->tables, s, c->stream), "twiddle tables");
+  nn_transform xa, xb;
+  nn_status st = xform_reserve(c, &xa, s);
+  if (st != NN_OK) return st;
+  const u64 row = 1ull << (s - plan[0].R);           // limbs a row of the first pass
+  const u64 full = na / row, part = na - full * row;  // full rows, limbs of the partial row
+  const u64 k = std::min<u64>(kInChunks, tiles);
+  cudaError_t e = cudaEventRecord(c->ev_first, c->stream);  // da and db are reused: after earlier work
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(c->copy, c->ev_first, 0);
+  for (u64 j = 0; j < k && e == cudaSuccess; ++j) {
+    const u64 t0 = tiles * j / k, t1 = tiles * (j + 1) / k, c0 = 16 * t0, c1 = 16 * t1;
+    if (full)
+      e = cudaMemcpy2DAsync(da + c0, row * 8, ha + c0, row * 8, (c1 - c0) * 8, full, cudaMemcpyHostToDevice, c->copy);
+    if (e == cudaSuccess && part > c0)
+      e = cudaMemcpyAsync(da + full * row + c0, ha + full * row + c0, (std::min(c1, part) - c0) * 8,
+                          cudaMemcpyHostToDevice, c->copy);
+    if (e == cudaSuccess) e = cudaEventRecord(c->ev_in, c->copy);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->ev_in, 0);
+    if (e == cudaSuccess) e = nn::ntt_first_pass_range(da, na, xa.res, s, c->tables, plan[0], t0, t1, c->stream);
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(db, hb, nb * 8, cudaMemcpyHostToDevice, c->copy);
+  if (e == cudaSuccess) e = cudaEventRecord(c->ev_second, c->copy);
+  if (e == cudaSuccess) e = nn::ntt_forward_tail(xa.res, s, c->tables, c->stream, plan);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->ev_second, 0);
+  if (e != cudaSuccess) st = fail(c, e, "first operand by column ranges");
+  if (st == NN_OK) st = forward_fused(c, &xb, db, nb, s, &xa);
+  if (st == NN_OK) st = inverse_save_to_host(c, &xb, d_out, na + nb, h_out);
   dev_free(c, xa.res, xa.words);
   dev_free(c, xb.res, xb.words);
   return st;
@@ -734,6 +782,7 @@ nn_status nn_context_create(int device, uint64_t budget, nn_context** out) {
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_first, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_second, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_chunk, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming);
   if (e == cudaSuccess) e = nn::upload_primes();
   if (e == cudaSuccess) {
     cudaMemPool_t pool;
@@ -748,6 +797,7 @@ nn_status nn_context_create(int device, uint64_t budget, nn_context** out) {
   if (e != cudaSuccess) {
     nn_status st = e == cudaErrorNoDevice || e == cudaErrorNoKernelImageForDevice ? NN_ERR_NO_DEVICE : NN_ERR_CUDA;
     cudaGetLastError();
+    if (c->ev_in) cudaEventDestroy(c->ev_in);
     if (c->ev_chunk) cudaEventDestroy(c->ev_chunk);
     if (c->ev_second) cudaEventDestroy(c->ev_second);
     if (c->ev_first) cudaEventDestroy(c->ev_first);
@@ -775,6 +825,7 @@ nn_status nn_context_destroy(nn_context* c) {
   nn::tables_free(c->tables);
   nn::scan_free(c->scan);
   cudaStreamSynchronize(c->copy);
+  cudaEventDestroy(c->ev_in);
   cudaEventDestroy(c->ev_chunk);
   cudaEventDestroy(c->ev_second);
   cudaEventDestroy(c->ev_first);
@@ -903,6 +954,18 @@ nn_status nn_mul_host(nn_context* c, uint64_t* out, uint64_t* out_n, const uint6
   if (st == NN_OK) st = scratch(c, 1, nb, &db);
   if (st == NN_OK) st = scratch(c, 2, na + nb, &dout);
   if (st != NN_OK) return st;
+  const int s = ntt_scale(na, nb);
+  if (nb >= kNttMulThreshold && s == ntt_scale((na + 1) >> 1, nb)) {  // balanced NTT product
+    bool used = false;
+    st = ntt_product_from_host(c, dout, da, a, na, db, b, nb, s, out, &used);
+    if (used || st != NN_OK) {
+      if (st == NN_OK) st = nn_context_synchronize(c);
+      const cudaError_t e = cudaStreamSynchronize(c->copy);
+      if (st == NN_OK && e != cudaSuccess) st = fail(c, e, "copy-back");
+      if (st == NN_OK && out_n) *out_n = normalized(out, na + nb);
+      return st;
+    }
+  }
   // a on the context's stream; b on the copy stream once a is in, so that
   // b's copy runs while a is transformed.
   NN_CK(c, cudaMemcpyAsync(da, a, na * 8, cudaMemcpyHostToDevice, c->stream), "H2D");

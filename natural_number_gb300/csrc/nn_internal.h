@@ -99,6 +99,16 @@ cudaError_t batch_configure(int* blocks_per_sm, size_t smem);
 cudaError_t batch_launch(const BatchJob* jobs, const BatchItem* items, u32 n_items, const u32* need, u32* done,
                          u32* head, u32* flags, u32* err, const Tables& t, int grid, size_t smem, cudaStream_t st);
 
+// The first forward pass a range of tiles at a time, so that it can start
+// on the columns of an operand already copied: *tiles receives the pass's
+// tile count, tile j covering columns [16 j, 16 j + 16) of every row of
+// 2^(s - R) limbs (false when the pass does not take this form).  Then
+// ntt_forward_tail runs the plan's other passes.
+bool ntt_first_pass_tiles(int s, const Pass& ps, u64* tiles);
+cudaError_t ntt_first_pass_range(const u64* limbs, u64 n, u64* res, int s, const Tables& t, const Pass& ps, u64 tile0,
+                                 u64 tile1, cudaStream_t st);
+cudaError_t ntt_forward_tail(u64* res, int s, const Tables& t, cudaStream_t st, const std::vector<Pass>& plan);
+
 // Forward transform: limbs (n <= 2^s) -> residues [3][2^s] equal to
 // NTT_info::load + NTT (ntt_info.h:147-198) modulo each prime; lazy values in
 // [0, 4p) for p0 and p1, [0, 2p) for p2.

@@ -232,10 +232,10 @@ __device__ __forceinline__ void load_tile_tma(u64* sm, const CUtensorMap* tm, co
 template <int BLOCKS, int THREADS>
 __global__ void __launch_bounds__(THREADS, BLOCKS) ntt_load_tma_kernel(const __grid_constant__ CUtensorMap tm, const u64* in,
                                                            u64 n_in, int s, int R, const u64* __restrict__ tab,
-                                                           u64 tab_stride) {
+                                                           u64 tab_stride, u64 tile0) {
   extern __shared__ __align__(128) u64 sm[];
   const int prime = (int)(blockIdx.x % 3);
-  const u64 tile = blockIdx.x / 3;
+  const u64 tile = tile0 + blockIdx.x / 3;
   const u64* tw = tab + prime * tab_stride;
   if (prime == 0)
     load_tile_tma<0>(sm, &tm, in, n_in, s, R, tw, tile);
@@ -471,9 +471,10 @@ cudaError_t launch_row_bulk(u64* out, int s, const Pass& ps, const Tables& t, cu
   return cudaGetLastError();
 }
 
+// Tiles [tile0, tile1) of the first pass (all of them by default).
 template <int BLOCKS, int THREADS>
 cudaError_t launch_load_tma(const CUtensorMap& tm, const u64* in, u64 n_in, int s, const Pass& ps, const Tables& t,
-                            cudaStream_t st) {
+                            cudaStream_t st, u64 tile0 = 0, u64 tile1 = ~0ull) {
   const size_t smem = ((size_t)16 << ps.R) * 8;
   static bool configured = false;
   if (!configured) {
@@ -482,10 +483,10 @@ cudaError_t launch_load_tma(const CUtensorMap& tm, const u64* in, u64 n_in, int 
     if (e != cudaSuccess) return e;
     configured = true;
   }
-  const u64 tiles = (1ull << s) / ((u64)16 << ps.R);
+  const u64 tiles = std::min<u64>((1ull << s) / ((u64)16 << ps.R), tile1) - tile0;
   launch_begin("ntt_fwd_load_col_pass", st);
   ntt_load_tma_kernel<BLOCKS, THREADS><<<(unsigned)(3 * tiles), THREADS, smem, st>>>(tm, in, n_in, s, ps.R, t.root,
-                                                                                     t.cap);
+                                                                                     t.cap, tile0);
   launch_end(st);
   return cudaGetLastError();
 }
@@ -649,6 +650,27 @@ cudaError_t ntt_forward_head(const u64* limbs, u64 n, u64* res, int s, const Tab
   for (size_t k = 0; k + 1 < plan.size(); ++k) {
     cudaError_t e = k == 0 ? dispatch_pass<true, false, false>(limbs, res, n, s, plan[k], t, st)
                            : dispatch_pass<false, false, false>(res, res, 0, s, plan[k], t, st);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+bool ntt_first_pass_tiles(int s, const Pass& ps, u64* tiles) {
+  if (ps.C != 16 || ps.lambda0 != 0 || s - ps.R < 4 || ps.R > 9 || !encode_tiled()) return false;
+  *tiles = (1ull << s) / ((u64)16 << ps.R);
+  return true;
+}
+
+cudaError_t ntt_first_pass_range(const u64* limbs, u64 n, u64* res, int s, const Tables& t, const Pass& ps, u64 tile0,
+                                 u64 tile1, cudaStream_t st) {
+  CUtensorMap tm;
+  if (!col_tensor_map(&tm, res, s, 0, ps.R)) return cudaErrorNotSupported;
+  return launch_load_tma<4, 256>(tm, limbs, n, s, ps, t, st, tile0, tile1);
+}
+
+cudaError_t ntt_forward_tail(u64* res, int s, const Tables& t, cudaStream_t st, const std::vector<Pass>& plan) {
+  for (size_t k = 1; k < plan.size(); ++k) {
+    cudaError_t e = dispatch_pass<false, false, false>(res, res, 0, s, plan[k], t, st);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;

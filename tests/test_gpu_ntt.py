@@ -153,11 +153,14 @@ def test_config2_large_multiply_and_square(ctx, golden):
             assert digest(normalize(sq)) == c["out"]
 
 
-@pytest.mark.parametrize("na,nb", [(1 << 16, 1 << 16), (50000, 3000), (200, 150), (70000, 65536)])
+@pytest.mark.parametrize("na,nb", [(1 << 16, 1 << 16), (50000, 3000), (200, 150), (70000, 65536), (300001, 200003),
+                                   (900001, 800003)])
 def test_mul_host_page_locked(ctx, oracle, na, nb):
     """Host products on page-locked operands and result (as the benchmark's
     end-to-end leg uses them), for the balanced NTT, split and base-case
-    paths, in both operand orders; and the same product from pageable arrays."""
+    paths, in both operand orders; and the same product from pageable arrays.
+    The balanced products copy the longer operand a column range at a time
+    while the first pass runs; odd lengths leave a partial last row."""
     import torch
     a, b = limbs(31 + na, na), limbs(37 + nb, nb)
     pa = torch.from_numpy(a).pin_memory().numpy()
