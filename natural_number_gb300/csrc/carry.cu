@@ -241,6 +241,27 @@ __global__ void __launch_bounds__(256) column_sums_kernel(ColumnProducer prod, u
   }
 }
 
+// One warp a job: lane i adds limb base + i of x and y; the block's carries
+// are those of the integer sum G + (G | P) + carry-in over the lanes' generate
+// and propagate bits (the same identity as the scan's warp step).
+__global__ void __launch_bounds__(256) add_batch_kernel(const AddJob* __restrict__ jobs, u64 m) {
+  const u64 j = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const u32 lane = threadIdx.x & 31;
+  if (j >= m) return;  // whole warps leave together
+  const AddJob J = jobs[j];
+  u32 carry = 0;
+  for (u64 base = 0; base < J.nout; base += 32) {
+    const u64 k = base + lane;
+    const u64 a = k < J.nx ? J.x[k] : 0, b = k < J.ny ? J.y[k] : 0;
+    const u64 sum = a + b;
+    const u32 G = __ballot_sync(0xffffffffu, sum < a), GP = __ballot_sync(0xffffffffu, sum < a || sum == ~0ull);
+    const u64 t = (u64)G + GP + carry;
+    const u32 cin = (((u32)t ^ G ^ GP) >> lane) & 1;
+    if (k < J.nout) J.out[k] = sum + cin;
+    carry = (u32)(t >> 32);
+  }
+}
+
 // Tiles [tile_begin, tile_end) of the scan (all of them by default).  The
 // ranges of one scan go in order on one stream (each range's carry-in comes
 // from the range before: through the status words of the lookback, or the
@@ -343,6 +364,14 @@ cudaError_t ntt_save_chunks(const u64* res, int s, u64* out, u64 size, Scan& sc,
     if (e == cudaSuccess) e = done(t0 * kScanTile, std::min(size, t1 * kScanTile));
   }
   return e;
+}
+
+cudaError_t add_batch(const AddJob* d_jobs, u64 m, cudaStream_t st) {
+  if (m == 0) return cudaSuccess;
+  launch_begin("add_batch", st);
+  add_batch_kernel<<<(unsigned)((m * 32 + 255) / 256), 256, 0, st>>>(d_jobs, m);
+  launch_end(st);
+  return cudaGetLastError();
 }
 
 cudaError_t school_mul(const u64* a, u64 na, const u64* b, u64 nb, u64* out, Scan& sc, cudaStream_t st) {

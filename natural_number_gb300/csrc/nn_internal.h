@@ -99,6 +99,20 @@ cudaError_t batch_configure(int* blocks_per_sm, size_t smem);
 cudaError_t batch_launch(const BatchJob* jobs, const BatchItem* items, u32 n_items, const u32* need, u32* done,
                          u32* head, u32* flags, u32* err, const Tables& t, int grid, size_t smem, cudaStream_t st);
 
+// Many sums at once (carry.cu): job j writes out = x + y in nout >=
+// max(nx, ny) + 1 limbs, one warp a job walking 32 limbs a step with the
+// carries of a step resolved by ballots.  For jobs of up to a few 10^4 limbs;
+// longer sums take lin_combine.
+struct AddJob {
+  const u64* x;
+  u64 nx;
+  const u64* y;
+  u64 ny;
+  u64* out;
+  u64 nout;
+};
+cudaError_t add_batch(const AddJob* d_jobs, u64 m, cudaStream_t st);
+
 // The first forward pass a range of tiles at a time, so that it can start
 // on the columns of an operand already copied: *tiles receives the pass's
 // tile count, tile j covering columns [16 j, 16 j + 16) of every row of

@@ -33,6 +33,7 @@
 
 #include "../../include/natural_gb300.h"
 #include "../../include/natural_gb300.hpp"
+#include "context_access.h"
 #include "nn_internal.h"
 
 namespace {
@@ -346,6 +347,118 @@ void run_products(nn_context* c, Products& P, Staging& stg, Stats& S) {
 }
 
 // ---------------------------------------------------------------------------
+// Device-resident tree levels: the levels above the host subtrees keep their
+// values in device memory; each level's products go to the GPU as one batch
+// on device pointers and its sums as one batched add, and only the root comes
+// back.  Values carry their product lengths (the top limbs may be zero).
+// ---------------------------------------------------------------------------
+
+struct DNum {  // n limbs at p in device memory
+  u64* p = nullptr;
+  u64 n = 0;
+};
+
+// The device memory of one tree level, released on the stream (after the
+// work queued on it) when the level is replaced.
+struct DLevel {
+  cudaStream_t st;
+  u64* p = nullptr;
+  u64 used = 0;
+  explicit DLevel(cudaStream_t s) : st(s) {}
+  DLevel(const DLevel&) = delete;
+  DLevel& operator=(DLevel&& o) noexcept {
+    if (this != &o) {
+      if (p) cudaFreeAsync(p, st);
+      st = o.st;
+      p = o.p;
+      used = o.used;
+      o.p = nullptr;
+    }
+    return *this;
+  }
+  ~DLevel() {
+    if (p) cudaFreeAsync(p, st);
+  }
+  static u64 words(u64 n) { return (n + 1) & ~1ull; }  // even offsets: 16-byte aligned values
+  void reserve(u64 w) { check_cuda(cudaMallocAsync((void**)&p, 8 * std::max<u64>(w, 2), st), "tree level"); }
+  DNum take(u64 n) {
+    DNum d{p + used, n};
+    used += words(n);
+    return d;
+  }
+};
+
+// Host naturals into a fresh level: packed into page-locked staging, one copy.
+void upload_level(DLevel& L, const std::vector<const natural*>& xs, std::vector<DNum>& out, Staging& stg) {
+  u64 w = 0;
+  for (const natural* x : xs) w += DLevel::words(x->size);
+  L.reserve(w);
+  out.resize(xs.size());
+  std::vector<u64> off(xs.size());
+  for (size_t k = 0; k < xs.size(); ++k) {
+    off[k] = L.used;
+    out[k] = L.take(xs[k]->size);
+  }
+  u64* h = stg.in.get(std::max<u64>(w, 1));
+  parallel_for(xs.size(), 256, [&](u64 k) { std::memcpy(h + off[k], xs[k]->data, 8 * xs[k]->size); });
+  check_cuda(cudaMemcpyAsync(L.p, h, 8 * w, cudaMemcpyHostToDevice, L.st), "tree upload");
+  // the staging is reused: the copy must have read it
+  check_cuda(cudaStreamSynchronize(L.st), "tree upload");
+}
+
+// Sums out = x + y: short ones in one batched launch (one warp a sum), long
+// ones one multiword scan each.
+constexpr u64 kWarpAddLimbs = 1 << 15;
+void device_adds(nn_context* c, const std::vector<nn::AddJob>& jobs) {
+  cudaStream_t st = (cudaStream_t)nn_context_stream(c);
+  std::vector<nn::AddJob> small;
+  for (const nn::AddJob& j : jobs) {
+    if (j.nout <= kWarpAddLimbs) {
+      small.push_back(j);
+      continue;
+    }
+    check_cuda(nn::lin_combine(j.out, j.nout - 1, j.x, j.nx, 0, j.y, j.ny, 0, false, 0, nn::ctx_scan(c), st),
+               "tree sum");
+  }
+  if (small.empty()) return;
+  DLevel tab(st);
+  const u64 w = (small.size() * sizeof(nn::AddJob) + 7) / 8;
+  tab.reserve(w);
+  // from pageable memory: the call returns once the table has been staged
+  check_cuda(cudaMemcpyAsync(tab.p, small.data(), small.size() * sizeof(nn::AddJob), cudaMemcpyHostToDevice, st),
+             "sum table");
+  check_cuda(nn::add_batch(reinterpret_cast<const nn::AddJob*>(tab.p), small.size(), st), "tree sums");
+}
+
+// One level's products as one batch on device pointers; the plan is released
+// by the caller once its run is no longer needed (releasing waits for it).
+nn_batch* device_products(nn_context* c, const std::vector<nn_mul_job>& jobs) {
+  std::vector<u64> na(jobs.size()), nb(jobs.size());
+  for (size_t k = 0; k < jobs.size(); ++k) {
+    na[k] = jobs[k].n_a;
+    nb[k] = jobs[k].n_b;
+  }
+  nn_batch* B = nullptr;
+  nn_status s = nn_batch_create(c, na.data(), nb.data(), nullptr, jobs.size(), &B);
+  if (s == NN_OK) s = nn_batch_launch(c, B, jobs.data());
+  if (s != NN_OK) {
+    if (B) nn_batch_destroy(c, B);
+    nn_gb300::check(s, "tree products");
+  }
+  return B;
+}
+
+// A device value back into a normalised natural (waits for the stream).
+natural download(nn_context* c, DNum d) {
+  natural x;
+  x.resize(d.n);
+  check_cuda(cudaMemcpyAsync(x.data, d.p, 8 * d.n, cudaMemcpyDeviceToHost, (cudaStream_t)nn_context_stream(c)),
+             "root download");
+  nn_gb300::check(nn_context_synchronize(c), "tree levels");
+  return std::move(x.std());
+}
+
+// ---------------------------------------------------------------------------
 // pi: calc_pi (natural.h:874-902) over terms [1, terms], terms a power of two
 // ---------------------------------------------------------------------------
 
@@ -433,28 +546,74 @@ void calc_pi_levels(nn_context* c, u64 terms, natural& num, natural& den, natura
   });
   S.host_s += since(t0);
   S.host_products += terms * 6 + (terms - nodes) * 4;
-  while (lv.size() > 1) {  // every level above the host subtrees (end - begin > 2)
-    const u64 m = lv.size() / 2;
-    std::vector<PiNode> up(m);
-    std::vector<natural> t1(m), t2(m);
-    Products P;
-    for (u64 j = 0; j < m; ++j) {
-      PiNode &L = lv[2 * j], &R = lv[2 * j + 1];
-      P.add(&t1[j], &R.den, &L.num);          // num = den1 * num
-      P.add(&t2[j], &L.numc, &R.num);         // num1 = numc * num1
-      P.add(&up[j].den, &R.den, &L.den);      // den = den1 * den
-      P.add(&up[j].numc, &L.numc, &R.numc);   // numc = numc * numc1
-    }
-    run_products(c, P, stg, S);
-    parallel_for(m, 64, [&](u64 j) { up[j].num = t1[j] + t2[j]; });
-    std::vector<PiNode> old;
-    old.swap(lv);
-    lv.swap(up);
-    parallel_for(old.size(), 256, [&](u64 k) { PiNode dead = std::move(old[k]); });
+  if (lv.size() == 1) {
+    num = std::move(lv[0].num);
+    den = std::move(lv[0].den);
+    numc = std::move(lv[0].numc);
+    return;
   }
-  num = std::move(lv[0].num);
-  den = std::move(lv[0].den);
-  numc = std::move(lv[0].numc);
+  // every level above the host subtrees (end - begin > 2), on the device
+  const auto tg = Clock::now();
+  cudaStream_t st = (cudaStream_t)nn_context_stream(c);
+  struct DPi {
+    DNum num, den, numc;
+  };
+  DLevel cur(st);
+  std::vector<DPi> dl(nodes);
+  {
+    std::vector<const natural*> xs;
+    for (const PiNode& nd : lv) {
+      xs.push_back(&nd.num);
+      xs.push_back(&nd.den);
+      xs.push_back(&nd.numc);
+    }
+    std::vector<DNum> d;
+    upload_level(cur, xs, d, stg);
+    for (u64 k = 0; k < nodes; ++k) dl[k] = DPi{d[3 * k], d[3 * k + 1], d[3 * k + 2]};
+    std::vector<PiNode>().swap(lv);
+  }
+  nn_batch* prev = nullptr;
+  while (dl.size() > 1) {
+    const u64 m = dl.size() / 2;
+    u64 w = 0;
+    for (u64 j = 0; j < m; ++j) {
+      const DPi &L = dl[2 * j], &R = dl[2 * j + 1];
+      const u64 n1 = R.den.n + L.num.n, n2 = L.numc.n + R.num.n;
+      w += DLevel::words(n1) + DLevel::words(n2) + DLevel::words(R.den.n + L.den.n) +
+           DLevel::words(L.numc.n + R.numc.n) + DLevel::words(std::max(n1, n2) + 1);
+    }
+    DLevel nxt(st);
+    nxt.reserve(w);
+    std::vector<DPi> up(m);
+    std::vector<nn_mul_job> jobs;
+    std::vector<nn::AddJob> sums(m);
+    jobs.reserve(4 * m);
+    for (u64 j = 0; j < m; ++j) {
+      const DPi &L = dl[2 * j], &R = dl[2 * j + 1];
+      const DNum t1 = nxt.take(R.den.n + L.num.n), t2 = nxt.take(L.numc.n + R.num.n);
+      up[j].den = nxt.take(R.den.n + L.den.n);
+      up[j].numc = nxt.take(L.numc.n + R.numc.n);
+      up[j].num = nxt.take(std::max(t1.n, t2.n) + 1);
+      jobs.push_back(nn_mul_job{R.den.p, R.den.n, L.num.p, L.num.n, t1.p});     // num = den1 * num
+      jobs.push_back(nn_mul_job{L.numc.p, L.numc.n, R.num.p, R.num.n, t2.p});   // num1 = numc * num1
+      jobs.push_back(nn_mul_job{R.den.p, R.den.n, L.den.p, L.den.n, up[j].den.p});      // den = den1 * den
+      jobs.push_back(nn_mul_job{L.numc.p, L.numc.n, R.numc.p, R.numc.n, up[j].numc.p});  // numc = numc * numc1
+      sums[j] = nn::AddJob{t1.p, t1.n, t2.p, t2.n, up[j].num.p, up[j].num.n};
+    }
+    nn_batch* plan = device_products(c, jobs);
+    device_adds(c, sums);
+    if (prev) nn_batch_destroy(c, prev);  // waits for the level before, while this one runs
+    prev = plan;
+    S.gpu_products += 4 * m;
+    S.batches += 1;
+    cur = std::move(nxt);
+    dl.swap(up);
+  }
+  if (prev) nn_batch_destroy(c, prev);
+  num = download(c, dl[0].num);
+  den = download(c, dl[0].den);
+  numc = download(c, dl[0].numc);
+  S.gpu_s += since(tg);
 }
 
 // ---------------------------------------------------------------------------
@@ -524,25 +683,67 @@ void calc_e_levels(nn_context* c, u64 terms, natural& num, natural& den, u64 hos
   });
   S.host_s += since(t0);
   S.host_products += pairs + (pairs - nodes) * 2;
-  while (lv.size() > 1) {
-    const u64 m = lv.size() / 2;
-    std::vector<ENode> up(m);
-    std::vector<natural> t(m);
-    Products P;
-    for (u64 j = 0; j < m; ++j) {
-      ENode &L = lv[2 * j], &R = lv[2 * j + 1];
-      P.add(&t[j], &R.den, &L.num);       // num = den1 * num
-      P.add(&up[j].den, &R.den, &L.den);  // den = den1 * den
-    }
-    run_products(c, P, stg, S);
-    parallel_for(m, 64, [&](u64 j) { up[j].num = t[j] + lv[2 * j + 1].num; });
-    std::vector<ENode> old;
-    old.swap(lv);
-    lv.swap(up);
-    parallel_for(old.size(), 256, [&](u64 k) { ENode dead = std::move(old[k]); });
+  if (lv.size() == 1) {
+    num = std::move(lv[0].num);
+    den = std::move(lv[0].den);
+    return;
   }
-  num = std::move(lv[0].num);
-  den = std::move(lv[0].den);
+  // the levels above the host subtrees, on the device
+  const auto tg = Clock::now();
+  cudaStream_t st = (cudaStream_t)nn_context_stream(c);
+  struct DE {
+    DNum num, den;
+  };
+  DLevel cur(st);
+  std::vector<DE> dl(nodes);
+  {
+    std::vector<const natural*> xs;
+    for (const ENode& nd : lv) {
+      xs.push_back(&nd.num);
+      xs.push_back(&nd.den);
+    }
+    std::vector<DNum> d;
+    upload_level(cur, xs, d, stg);
+    for (u64 k = 0; k < nodes; ++k) dl[k] = DE{d[2 * k], d[2 * k + 1]};
+    std::vector<ENode>().swap(lv);
+  }
+  nn_batch* prev = nullptr;
+  while (dl.size() > 1) {
+    const u64 m = dl.size() / 2;
+    u64 w = 0;
+    for (u64 j = 0; j < m; ++j) {
+      const DE &L = dl[2 * j], &R = dl[2 * j + 1];
+      const u64 nt = R.den.n + L.num.n;
+      w += DLevel::words(nt) + DLevel::words(R.den.n + L.den.n) + DLevel::words(std::max(nt, R.num.n) + 1);
+    }
+    DLevel nxt(st);
+    nxt.reserve(w);
+    std::vector<DE> up(m);
+    std::vector<nn_mul_job> jobs;
+    std::vector<nn::AddJob> sums(m);
+    jobs.reserve(2 * m);
+    for (u64 j = 0; j < m; ++j) {
+      const DE &L = dl[2 * j], &R = dl[2 * j + 1];
+      const DNum t = nxt.take(R.den.n + L.num.n);
+      up[j].den = nxt.take(R.den.n + L.den.n);
+      up[j].num = nxt.take(std::max(t.n, R.num.n) + 1);
+      jobs.push_back(nn_mul_job{R.den.p, R.den.n, L.num.p, L.num.n, t.p});          // num = den1 * num
+      jobs.push_back(nn_mul_job{R.den.p, R.den.n, L.den.p, L.den.n, up[j].den.p});  // den = den1 * den
+      sums[j] = nn::AddJob{t.p, t.n, R.num.p, R.num.n, up[j].num.p, up[j].num.n};   // ... + num1
+    }
+    nn_batch* plan = device_products(c, jobs);
+    device_adds(c, sums);
+    if (prev) nn_batch_destroy(c, prev);
+    prev = plan;
+    S.gpu_products += 2 * m;
+    S.batches += 1;
+    cur = std::move(nxt);
+    dl.swap(up);
+  }
+  if (prev) nn_batch_destroy(c, prev);
+  num = download(c, dl[0].num);
+  den = download(c, dl[0].den);
+  S.gpu_s += since(tg);
 }
 
 // ---------------------------------------------------------------------------
