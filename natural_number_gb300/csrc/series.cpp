@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <condition_variable>
 #include <cstdio>
 #include <cstring>
 #include <exception>
@@ -353,6 +354,8 @@ void run_products(nn_context* c, Products& P, Staging& stg, Stats& S) {
 // back.  Values carry their product lengths (the top limbs may be zero).
 // ---------------------------------------------------------------------------
 
+constexpr u64 kTreeSlabs = 8;  // pi's host subtrees come in this many slabs
+
 struct DNum {  // n limbs at p in device memory
   u64* p = nullptr;
   u64 n = 0;
@@ -366,6 +369,7 @@ struct DLevel {
   u64 used = 0;
   explicit DLevel(cudaStream_t s) : st(s) {}
   DLevel(const DLevel&) = delete;
+  DLevel(DLevel&& o) noexcept : st(o.st), p(o.p), used(o.used) { o.p = nullptr; }
   DLevel& operator=(DLevel&& o) noexcept {
     if (this != &o) {
       if (p) cudaFreeAsync(p, st);
@@ -388,8 +392,12 @@ struct DLevel {
   }
 };
 
-// Host naturals into a fresh level: packed into page-locked staging, one copy.
-void upload_level(DLevel& L, const std::vector<const natural*>& xs, std::vector<DNum>& out, Staging& stg) {
+// Host naturals into a fresh level: packed into the page-locked buffer `buf`,
+// one copy.  `copied` marks the end of the buffer's last copy: the packing
+// waits for it (and for nothing else queued on the stream), and it is
+// recorded again after this copy.
+void upload_level(DLevel& L, const std::vector<const natural*>& xs, std::vector<DNum>& out, Pinned& buf,
+                  cudaEvent_t copied) {
   u64 w = 0;
   for (const natural* x : xs) w += DLevel::words(x->size);
   L.reserve(w);
@@ -399,12 +407,21 @@ void upload_level(DLevel& L, const std::vector<const natural*>& xs, std::vector<
     off[k] = L.used;
     out[k] = L.take(xs[k]->size);
   }
-  u64* h = stg.in.get(std::max<u64>(w, 1));
+  check_cuda(cudaEventSynchronize(copied), "staging reuse");
+  u64* h = buf.get(std::max<u64>(w, 1));
   parallel_for(xs.size(), 256, [&](u64 k) { std::memcpy(h + off[k], xs[k]->data, 8 * xs[k]->size); });
   check_cuda(cudaMemcpyAsync(L.p, h, 8 * w, cudaMemcpyHostToDevice, L.st), "tree upload");
-  // the staging is reused: the copy must have read it
-  check_cuda(cudaStreamSynchronize(L.st), "tree upload");
+  check_cuda(cudaEventRecord(copied, L.st), "tree upload");
 }
+
+struct Event {  // a CUDA event for the duration of a scope
+  cudaEvent_t e = nullptr;
+  Event() { check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event"); }
+  Event(const Event&) = delete;
+  ~Event() {
+    if (e) cudaEventDestroy(e);
+  }
+};
 
 // Sums out = x + y: short ones in one batched launch (one warp a sum), long
 // ones one multiword scan each.
@@ -529,50 +546,15 @@ struct PiNode {
   natural num, den, numc;
 };
 
-void calc_pi_levels(nn_context* c, u64 terms, natural& num, natural& den, natural& numc, u64 host_below,
-                    Staging& stg, Stats& S) {
-  // subtrees of `chunk` terms on the host: their den reaches about host_below limbs
-  const u64 chunk = std::min(std::bit_floor(std::max<u64>(2, host_below / 2)), terms);
-  const u64 nodes = terms / chunk;
-  std::vector<PiNode> lv(nodes);
-  const auto t0 = Clock::now();
-  parallel_for(nodes, 1, [&](u64 k) {
-    const u64 cn = pi_cap_num(chunk), cd = pi_cap_den(chunk), cc = pi_cap_numc(chunk);
-    u64* w = scratch_words(cn + cd + cc + pi_scratch(chunk));
-    const Len3 r = pi_subtree(1 + k * chunk, chunk, w, w + cn, w + cn + cd, w + cn + cd + cc);
-    lv[k].num = to_natural(w, r.num);
-    lv[k].den = to_natural(w + cn, r.den);
-    lv[k].numc = to_natural(w + cn + cd, r.numc);
-  });
-  S.host_s += since(t0);
-  S.host_products += terms * 6 + (terms - nodes) * 4;
-  if (lv.size() == 1) {
-    num = std::move(lv[0].num);
-    den = std::move(lv[0].den);
-    numc = std::move(lv[0].numc);
-    return;
-  }
-  // every level above the host subtrees (end - begin > 2), on the device
-  const auto tg = Clock::now();
+struct DPi {
+  DNum num, den, numc;
+};
+
+// Levels on the device until one node is left: dl's values live in `cur`
+// (or in arenas the caller keeps); each level's plan goes to `plans`, to be
+// released once its run is over (releasing waits for the run).
+void pi_reduce(nn_context* c, std::vector<DPi>& dl, DLevel& cur, std::vector<nn_batch*>& plans, Stats& S) {
   cudaStream_t st = (cudaStream_t)nn_context_stream(c);
-  struct DPi {
-    DNum num, den, numc;
-  };
-  DLevel cur(st);
-  std::vector<DPi> dl(nodes);
-  {
-    std::vector<const natural*> xs;
-    for (const PiNode& nd : lv) {
-      xs.push_back(&nd.num);
-      xs.push_back(&nd.den);
-      xs.push_back(&nd.numc);
-    }
-    std::vector<DNum> d;
-    upload_level(cur, xs, d, stg);
-    for (u64 k = 0; k < nodes; ++k) dl[k] = DPi{d[3 * k], d[3 * k + 1], d[3 * k + 2]};
-    std::vector<PiNode>().swap(lv);
-  }
-  nn_batch* prev = nullptr;
   while (dl.size() > 1) {
     const u64 m = dl.size() / 2;
     u64 w = 0;
@@ -594,25 +576,147 @@ void calc_pi_levels(nn_context* c, u64 terms, natural& num, natural& den, natura
       up[j].den = nxt.take(R.den.n + L.den.n);
       up[j].numc = nxt.take(L.numc.n + R.numc.n);
       up[j].num = nxt.take(std::max(t1.n, t2.n) + 1);
-      jobs.push_back(nn_mul_job{R.den.p, R.den.n, L.num.p, L.num.n, t1.p});     // num = den1 * num
-      jobs.push_back(nn_mul_job{L.numc.p, L.numc.n, R.num.p, R.num.n, t2.p});   // num1 = numc * num1
-      jobs.push_back(nn_mul_job{R.den.p, R.den.n, L.den.p, L.den.n, up[j].den.p});      // den = den1 * den
+      jobs.push_back(nn_mul_job{R.den.p, R.den.n, L.num.p, L.num.n, t1.p});              // num = den1 * num
+      jobs.push_back(nn_mul_job{L.numc.p, L.numc.n, R.num.p, R.num.n, t2.p});            // num1 = numc * num1
+      jobs.push_back(nn_mul_job{R.den.p, R.den.n, L.den.p, L.den.n, up[j].den.p});       // den = den1 * den
       jobs.push_back(nn_mul_job{L.numc.p, L.numc.n, R.numc.p, R.numc.n, up[j].numc.p});  // numc = numc * numc1
       sums[j] = nn::AddJob{t1.p, t1.n, t2.p, t2.n, up[j].num.p, up[j].num.n};
     }
-    nn_batch* plan = device_products(c, jobs);
+    plans.push_back(device_products(c, jobs));
     device_adds(c, sums);
-    if (prev) nn_batch_destroy(c, prev);  // waits for the level before, while this one runs
-    prev = plan;
     S.gpu_products += 4 * m;
     S.batches += 1;
     cur = std::move(nxt);
     dl.swap(up);
   }
-  if (prev) nn_batch_destroy(c, prev);
-  num = download(c, dl[0].num);
-  den = download(c, dl[0].den);
-  numc = download(c, dl[0].numc);
+}
+
+void release_plans(nn_context* c, std::vector<nn_batch*>& plans) {
+  for (nn_batch* B : plans) nn_batch_destroy(c, B);
+  plans.clear();
+}
+
+// calc_pi over [1, terms]: the bottom subtrees on host threads, the levels
+// above them on the device.  The subtrees come in slabs, computed by a
+// producer thread (with all host cores) while this thread hands the slabs
+// before to the device (whose calls may wait for the GPU); each slab is
+// reduced to its root on the device, and the roots meet in the top levels.
+void calc_pi_levels(nn_context* c, u64 terms, natural& num, natural& den, natural& numc, u64 host_below,
+                    Staging& stg, Stats& S) {
+  // subtrees of `chunk` terms on the host: their den reaches about host_below limbs
+  const u64 chunk = std::min(std::bit_floor(std::max<u64>(2, host_below / 2)), terms);
+  const u64 nodes = terms / chunk;
+  S.host_products += terms * 6 + (terms - nodes) * 4;
+  std::atomic<u64> host_ns{0};
+  auto subtrees = [&](u64 k0, u64 q, std::vector<PiNode>& lv) {
+    const auto t0 = Clock::now();
+    lv.assign(q, PiNode{});
+    parallel_for(q, 1, [&](u64 i) {
+      const u64 cn = pi_cap_num(chunk), cd = pi_cap_den(chunk), cc = pi_cap_numc(chunk);
+      u64* w = scratch_words(cn + cd + cc + pi_scratch(chunk));
+      const Len3 r = pi_subtree(1 + (k0 + i) * chunk, chunk, w, w + cn, w + cn + cd, w + cn + cd + cc);
+      lv[i].num = to_natural(w, r.num);
+      lv[i].den = to_natural(w + cn, r.den);
+      lv[i].numc = to_natural(w + cn + cd, r.numc);
+    });
+    host_ns += (u64)(since(t0) * 1e9);
+  };
+  if (nodes == 1) {
+    std::vector<PiNode> lv;
+    subtrees(0, 1, lv);
+    S.host_s += host_ns * 1e-9;
+    num = std::move(lv[0].num);
+    den = std::move(lv[0].den);
+    numc = std::move(lv[0].numc);
+    return;
+  }
+  const auto tg = Clock::now();
+  cudaStream_t st = (cudaStream_t)nn_context_stream(c);
+  const u64 slabs = std::min<u64>(kTreeSlabs, nodes / 2), q = nodes / slabs;  // powers of two
+  // the producer: slab after slab into `ready`; `stop` ends it early
+  std::vector<std::vector<PiNode>> ready(slabs);
+  std::mutex mu;
+  std::condition_variable cv;
+  u64 produced = 0;
+  bool stop = false;
+  std::exception_ptr perr;
+  std::thread producer([&] {
+    for (u64 sl = 0; sl < slabs; ++sl) {
+      {
+        std::lock_guard<std::mutex> g(mu);
+        if (stop) return;
+      }
+      try {
+        subtrees(sl * q, q, ready[sl]);
+      } catch (...) {
+        std::lock_guard<std::mutex> g(mu);
+        perr = std::current_exception();
+        produced = slabs;
+        cv.notify_all();
+        return;
+      }
+      std::lock_guard<std::mutex> g(mu);
+      produced = sl + 1;
+      cv.notify_all();
+    }
+  });
+  struct Join {  // the producer ends before this function does, however it is left
+    std::thread& t;
+    std::mutex& mu;
+    bool& stop;
+    ~Join() {
+      {
+        std::lock_guard<std::mutex> g(mu);
+        stop = true;
+      }
+      if (t.joinable()) t.join();
+    }
+  } join{producer, mu, stop};
+  Event copied[2];
+  std::vector<DLevel> slab_mem;  // each slab's last level, holding its root
+  slab_mem.reserve(slabs);
+  std::vector<DPi> roots(slabs);
+  std::vector<nn_batch*> plans[3];
+  struct Release {  // every plan is released, however the function is left
+    nn_context* c;
+    std::vector<nn_batch*>* p;
+    ~Release() {
+      for (int i = 0; i < 3; ++i) release_plans(c, p[i]);
+    }
+  } release{c, plans};
+  for (u64 sl = 0; sl < slabs; ++sl) {
+    {
+      std::unique_lock<std::mutex> g(mu);
+      cv.wait(g, [&] { return produced > sl; });
+      if (perr) std::rethrow_exception(perr);
+    }
+    std::vector<PiNode> lv;
+    lv.swap(ready[sl]);
+    DLevel cur(st);
+    std::vector<DPi> dl(q);
+    {
+      std::vector<const natural*> xs;
+      for (const PiNode& nd : lv) {
+        xs.push_back(&nd.num);
+        xs.push_back(&nd.den);
+        xs.push_back(&nd.numc);
+      }
+      std::vector<DNum> d;
+      upload_level(cur, xs, d, sl % 2 ? stg.out : stg.in, copied[sl % 2].e);
+      for (u64 k = 0; k < q; ++k) dl[k] = DPi{d[3 * k], d[3 * k + 1], d[3 * k + 2]};
+    }
+    std::vector<nn_batch*>& mine = plans[sl % 3];
+    release_plans(c, mine);  // slab sl - 3's: long done
+    pi_reduce(c, dl, cur, mine, S);
+    roots[sl] = dl[0];
+    slab_mem.push_back(std::move(cur));
+  }
+  DLevel top(st);
+  pi_reduce(c, roots, top, plans[slabs % 3], S);
+  num = download(c, roots[0].num);
+  den = download(c, roots[0].den);
+  numc = download(c, roots[0].numc);
+  S.host_s += host_ns * 1e-9;
   S.gpu_s += since(tg);
 }
 
@@ -703,8 +807,10 @@ void calc_e_levels(nn_context* c, u64 terms, natural& num, natural& den, u64 hos
       xs.push_back(&nd.den);
     }
     std::vector<DNum> d;
-    upload_level(cur, xs, d, stg);
+    Event copied;
+    upload_level(cur, xs, d, stg.in, copied.e);
     for (u64 k = 0; k < nodes; ++k) dl[k] = DE{d[2 * k], d[2 * k + 1]};
+    check_cuda(cudaEventSynchronize(copied.e), "tree upload");  // the staging is reused later
     std::vector<ENode>().swap(lv);
   }
   nn_batch* prev = nullptr;
