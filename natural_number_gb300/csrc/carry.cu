@@ -243,16 +243,18 @@ __global__ void __launch_bounds__(256) column_sums_kernel(ColumnProducer prod, u
 
 // One warp a job: lane i adds limb base + i of x and y; the block's carries
 // are those of the integer sum G + (G | P) + carry-in over the lanes' generate
-// and propagate bits (the same identity as the scan's warp step).
+// and propagate bits (the same identity as the scan's warp step).  A
+// difference adds the complement of y with a carry-in of 1.
 __global__ void __launch_bounds__(256) add_batch_kernel(const AddJob* __restrict__ jobs, u64 m) {
   const u64 j = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const u32 lane = threadIdx.x & 31;
   if (j >= m) return;  // whole warps leave together
   const AddJob J = jobs[j];
-  u32 carry = 0;
+  const u64 flip = J.sub ? ~0ull : 0;
+  u32 carry = J.sub ? 1 : 0;
   for (u64 base = 0; base < J.nout; base += 32) {
     const u64 k = base + lane;
-    const u64 a = k < J.nx ? J.x[k] : 0, b = k < J.ny ? J.y[k] : 0;
+    const u64 a = k < J.nx ? J.x[k] : 0, b = (k < J.ny ? J.y[k] : 0) ^ flip;
     const u64 sum = a + b;
     const u32 G = __ballot_sync(0xffffffffu, sum < a), GP = __ballot_sync(0xffffffffu, sum < a || sum == ~0ull);
     const u64 t = (u64)G + GP + carry;

@@ -18,9 +18,9 @@
 // quotient limbs at once.  A division costs two passes over a segment plus
 // five compositions instead of one pass over the whole node.
 //
-// Layout: node k's limbs at w[k * stride ...), copied into shared memory,
-// divided there; its digits go to out[k * width, (k + 1) * width), width =
-// 18 * groups, most significant group first.
+// Layout: node k's len[k] limbs at nodes[k], copied into `stride` limbs of
+// shared memory and divided there; its digits go to out[k * width, (k + 1) *
+// width), width = 18 * groups, most significant group first.
 #include <cuda_runtime.h>
 
 #include "nn_device.cuh"
@@ -94,7 +94,7 @@ __constant__ u64 c_limb_pow[kMaxSegment + 1];
 // One warp a node; `per_cta` warps a CTA, each with `stride` limbs of shared
 // memory.  A division pass over the current m limbs: segments of
 // ceil(m / 32) limbs, lane l holding limbs [l * seg, (l + 1) * seg).
-__global__ void __launch_bounds__(128) dec_groups_kernel(const u64* __restrict__ w, u64 stride,
+__global__ void __launch_bounds__(128) dec_groups_kernel(const u64* const* __restrict__ nodes, u64 stride,
                                                          const u32* __restrict__ len, u64 n, u32 groups, u64 v,
                                                          char* out) {
   extern __shared__ u64 node_sm[];
@@ -103,7 +103,8 @@ __global__ void __launch_bounds__(128) dec_groups_kernel(const u64* __restrict__
   if (k >= n) return;  // a whole warp leaves together
   u64* a = node_sm + (u64)warp * stride;
   u32 m = len[k];
-  for (u32 j = lane; j < m; j += 32) a[j] = w[k * stride + j];
+  const u64* w = nodes[k];
+  for (u32 j = lane; j < m; j += 32) a[j] = w[j];
   __syncwarp();
   char* o = out + k * (u64)groups * 18;
   for (u32 g = groups; g-- > 0;) {
@@ -146,9 +147,82 @@ __global__ void __launch_bounds__(128) dec_groups_kernel(const u64* __restrict__
   }
 }
 
+// out = in >> shift bits (n_out limbs, in read as zero past n_in): block
+// (x, y) covers limbs [x * 4096, x * 4096 + 4096) of job y.
+__global__ void __launch_bounds__(256) shr_batch_kernel(const ShrJob* __restrict__ jobs) {
+  const ShrJob J = jobs[blockIdx.y];
+  const u64 ls = J.shift >> 6;
+  const u32 bs = (u32)(J.shift & 63);
+  for (u64 t = (u64)blockIdx.x * kShrChunk + threadIdx.x; t < J.n_out && t < (u64)(blockIdx.x + 1) * kShrChunk;
+       t += blockDim.x) {
+    const u64 i = t + ls;
+    const u64 a = i < J.n_in ? J.in[i] : 0, b = i + 1 < J.n_in ? J.in[i + 1] : 0;
+    J.out[t] = bs ? (a >> bs) | (b << (64 - bs)) : a;
+  }
+}
+
+// One warp: x (nx limbs) against y (ny limbs): -1, 0 or 1.
+__device__ int warp_cmp(const u64* x, u64 nx, const u64* y, u64 ny, u32 lane) {
+  const u64 n = nx > ny ? nx : ny;
+  for (u64 top = (n + 31) & ~31ull; top > 0; top -= 32) {
+    const u64 k = top - 32 + lane;
+    const u64 a = k < nx ? x[k] : 0, b = k < ny ? y[k] : 0;
+    const u32 d = __ballot_sync(0xffffffffu, a != b);
+    if (d) {
+      const int hl = 31 - __clz(d);
+      const int gt = __shfl_sync(0xffffffffu, a > b ? 1 : 0, hl);
+      return gt ? 1 : -1;
+    }
+  }
+  return 0;
+}
+
+// One warp: x (n limbs) += y (or -= y with `sub`), carries by ballots; past
+// y's limbs the walk ends once no carry (borrow) is left.
+__device__ void warp_addsub(u64* x, u64 n, const u64* y, u64 ny, bool sub, u32 lane) {
+  const u64 flip = sub ? ~0ull : 0;
+  const u32 idle = sub ? 1 : 0;  // the carry word when nothing is pending
+  u32 carry = idle;
+  for (u64 base = 0; base < n; base += 32) {
+    if (base >= ny && carry == idle) break;
+    const u64 k = base + lane;
+    const u64 a = k < n ? x[k] : 0, b = (k < ny ? y[k] : 0) ^ flip;
+    const u64 sum = a + b;
+    const u32 G = __ballot_sync(0xffffffffu, sum < a), GP = __ballot_sync(0xffffffffu, sum < a || sum == ~0ull);
+    const u64 t = (u64)G + GP + carry;
+    if (k < n) x[k] = sum + ((((u32)t ^ G ^ GP) >> lane) & 1);
+    carry = (u32)(t >> 32);
+  }
+}
+
+// The split's correction (natural.h:962-965): while lo >= base, hi += 1 and
+// lo -= base, at most kMaxFix times (an error otherwise); zero[k] = hi == 0.
+constexpr int kMaxFix = 8;
+__global__ void __launch_bounds__(256) dec_fix_kernel(const DecFixJob* __restrict__ jobs, u64 m, const u64* base,
+                                                      u64 nb, u32* zero, u32* err) {
+  const u64 k = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const u32 lane = threadIdx.x & 31;
+  if (k >= m) return;  // whole warps leave together
+  const DecFixJob J = jobs[k];
+  const u64 one = 1;
+  int it = 0;
+  for (; it < kMaxFix && warp_cmp(J.lo, J.n_lo, base, nb, lane) >= 0; ++it) {
+    warp_addsub(J.lo, J.n_lo, base, nb, true, lane);
+    __syncwarp();
+    warp_addsub(J.hi, J.n_hi, &one, 1, false, lane);
+    __syncwarp();
+  }
+  if (it == kMaxFix && lane == 0) atomicExch(err, 1u);
+  u32 nz = 0;
+  for (u64 i = lane; i < J.n_hi; i += 32) nz |= J.hi[i] != 0;
+  nz = __any_sync(0xffffffffu, nz);
+  if (lane == 0) zero[k] = !nz;
+}
+
 }  // namespace
 
-cudaError_t dec_groups(const u64* w, u64 stride, const u32* len, u64 n, u32 groups, char* out, cudaStream_t st) {
+cudaError_t dec_groups(const u64* const* nodes, u64 stride, const u32* len, u64 n, u32 groups, char* out,
+                       cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   if (stride > (u64)32 * kMaxSegment || stride % 2) return cudaErrorInvalidValue;
   // 2^(64 j) mod 10^18 into the constant bank, once per device (each device
@@ -176,8 +250,28 @@ cudaError_t dec_groups(const u64* w, u64 stride, const u32* len, u64 n, u32 grou
     if (e != cudaSuccess) return e;
   }
   launch_begin("dec_groups", st);
-  dec_groups_kernel<<<(unsigned)((n + per_cta - 1) / per_cta), 32 * per_cta, smem, st>>>(w, stride, len, n, groups, v,
-                                                                                          out);
+  dec_groups_kernel<<<(unsigned)((n + per_cta - 1) / per_cta), 32 * per_cta, smem, st>>>(nodes, stride, len, n, groups,
+                                                                                          v, out);
+  launch_end(st);
+  return cudaGetLastError();
+}
+
+cudaError_t shr_batch(const ShrJob* d_jobs, const std::vector<ShrJob>& jobs, cudaStream_t st) {
+  u64 chunks = 1;
+  for (const ShrJob& j : jobs) chunks = std::max<u64>(chunks, (j.n_out + kShrChunk - 1) / kShrChunk);
+  for (u64 j0 = 0; j0 < jobs.size(); j0 += 65535) {  // grid y holds at most 65535 jobs
+    const unsigned ny = (unsigned)std::min<u64>(65535, jobs.size() - j0);
+    launch_begin("dec_shift", st);
+    shr_batch_kernel<<<dim3((unsigned)chunks, ny), 256, 0, st>>>(d_jobs + j0);
+    launch_end(st);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t dec_fix(const DecFixJob* d_jobs, u64 m, const u64* base, u64 nb, u32* zero, u32* err, cudaStream_t st) {
+  if (m == 0) return cudaSuccess;
+  launch_begin("dec_fix", st);
+  dec_fix_kernel<<<(unsigned)((m * 32 + 255) / 256), 256, 0, st>>>(d_jobs, m, base, nb, zero, err);
   launch_end(st);
   return cudaGetLastError();
 }

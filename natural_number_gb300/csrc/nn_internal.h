@@ -100,9 +100,10 @@ cudaError_t batch_launch(const BatchJob* jobs, const BatchItem* items, u32 n_ite
                          u32* head, u32* flags, u32* err, const Tables& t, int grid, size_t smem, cudaStream_t st);
 
 // Many sums at once (carry.cu): job j writes out = x + y in nout >=
-// max(nx, ny) + 1 limbs, one warp a job walking 32 limbs a step with the
-// carries of a step resolved by ballots.  For jobs of up to a few 10^4 limbs;
-// longer sums take lin_combine.
+// max(nx, ny) + 1 limbs, or with `sub` out = x - y mod B^nout (x >= y: the
+// difference), one warp a job walking 32 limbs a step with the carries of a
+// step resolved by ballots.  For jobs of up to a few 10^4 limbs; longer sums
+// take lin_combine.
 struct AddJob {
   const u64* x;
   u64 nx;
@@ -110,6 +111,7 @@ struct AddJob {
   u64 ny;
   u64* out;
   u64 nout;
+  u64 sub = 0;
 };
 cudaError_t add_batch(const AddJob* d_jobs, u64 m, cudaStream_t st);
 
@@ -173,11 +175,34 @@ cudaError_t shr_bits(u64* out, const u64* in, u64 n, unsigned cl, cudaStream_t s
 // most `limit` polls); it gives up and sets sc.err, which the host reads.
 cudaError_t wait_probe(Scan& sc, int limit, cudaStream_t st);
 
+// The decimal split on the device (decimal.cu): out = in >> shift bits for
+// many jobs (n_out limbs each, in read as zero past n_in); and the split's
+// correction (natural.h:962-965): while lo >= base, hi += 1 and lo -= base,
+// one warp a node, with zero[k] = (hi == 0) after it and *err set when a node
+// needed more than 8 steps.
+constexpr u64 kShrChunk = 4096;
+struct ShrJob {
+  const u64* in;
+  u64 n_in;
+  u64* out;
+  u64 n_out;
+  u64 shift;
+};
+cudaError_t shr_batch(const ShrJob* d_jobs, const std::vector<ShrJob>& jobs, cudaStream_t st);
+struct DecFixJob {
+  u64* lo;
+  u64 n_lo;
+  u64* hi;
+  u64 n_hi;
+};
+cudaError_t dec_fix(const DecFixJob* d_jobs, u64 m, const u64* base, u64 nb, u32* zero, u32* err, cudaStream_t st);
+
 // Decimal digits of n short naturals at once (decimal.cu): node k's len[k]
-// limbs at w[k * stride ...) (stride even, at most 8192); node k < 10^(18 *
-// groups) goes to out[k * 18 * groups ...) as 18 * groups zero-padded
-// digits, most significant first.
-cudaError_t dec_groups(const u64* w, u64 stride, const u32* len, u64 n, u32 groups, char* out, cudaStream_t st);
+// limbs at nodes[k] (device pointers; len[k] <= stride, stride even and at
+// most 8192); node k < 10^(18 * groups) goes to out[k * 18 * groups ...) as
+// 18 * groups zero-padded digits, most significant first.
+cudaError_t dec_groups(const u64* const* nodes, u64 stride, const u32* len, u64 n, u32 groups, char* out,
+                       cudaStream_t st);
 
 // Launch accounting (profile.cpp): every launch site brackets its kernel.
 void launch_begin(const char* name, cudaStream_t st);

@@ -247,106 +247,6 @@ struct Staging {
   Pinned in, out;
 };
 
-// Products out[k] = a[k] * b[k] of nonzero naturals, computed as one batch on the GPU.
-struct Products {
-  std::vector<const natural*> a, b;
-  std::vector<natural*> out;
-  void add(natural* o, const natural* x, const natural* y) {
-    a.push_back(x);
-    b.push_back(y);
-    out.push_back(o);
-  }
-  u64 size() const { return out.size(); }
-};
-
-// Operands and products at least this long cross the host link straight
-// from and into their own buffers (the drop-in natural keeps those
-// page-locked); shorter ones are packed into the staging, one copy each way.
-constexpr u64 kDirectLimbs = 1 << 14;
-
-void run_products(nn_context* c, Products& P, Staging& stg, Stats& S) {
-  const u64 m = P.size();
-  if (!m) return;
-  const auto t0 = Clock::now();
-  std::vector<u64> na(m), nb(m), oa(m), ob(m), oo(m);
-  // device layout: the short operands (and products) packed first, so that
-  // one copy moves them; the long ones after
-  u64 tin = 0, tout = 0;
-  for (int pass = 0; pass < 2; ++pass)
-    for (u64 k = 0; k < m; ++k) {
-      na[k] = P.a[k]->size;
-      nb[k] = P.b[k]->size;
-      // even offsets: the kernels read 16-byte aligned operands with vector loads
-      if ((na[k] >= kDirectLimbs) == (pass == 1)) {
-        oa[k] = tin;
-        tin = (tin + na[k] + 1) & ~1ull;
-      }
-      if ((nb[k] >= kDirectLimbs) == (pass == 1)) {
-        ob[k] = tin;
-        tin = (tin + nb[k] + 1) & ~1ull;
-      }
-      if ((na[k] + nb[k] >= kDirectLimbs) == (pass == 1)) {
-        oo[k] = tout;
-        tout = (tout + na[k] + nb[k] + 1) & ~1ull;
-      }
-    }
-  u64 tin_small = 0, tout_small = 0;
-  for (u64 k = 0; k < m; ++k) {
-    if (na[k] < kDirectLimbs) tin_small = std::max(tin_small, oa[k] + na[k]);
-    if (nb[k] < kDirectLimbs) tin_small = std::max(tin_small, ob[k] + nb[k]);
-    if (na[k] + nb[k] < kDirectLimbs) tout_small = std::max(tout_small, oo[k] + na[k] + nb[k]);
-  }
-  u64* hin = stg.in.get(std::max<u64>(tin_small, 1));
-  u64* hout = stg.out.get(std::max<u64>(tout_small, 1));
-  parallel_for(m, 256, [&](u64 k) {
-    if (na[k] < kDirectLimbs) std::memcpy(hin + oa[k], P.a[k]->data, 8 * na[k]);
-    if (nb[k] < kDirectLimbs) std::memcpy(hin + ob[k], P.b[k]->data, 8 * nb[k]);
-  });
-  cudaStream_t st = (cudaStream_t)nn_context_stream(c);
-  u64 *din = nullptr, *dout = nullptr;
-  check_cuda(cudaMallocAsync((void**)&din, 8 * tin, st), "batch operands");
-  check_cuda(cudaMallocAsync((void**)&dout, 8 * tout, st), "batch products");
-  if (tin_small) check_cuda(cudaMemcpyAsync(din, hin, 8 * tin_small, cudaMemcpyHostToDevice, st), "upload");
-  for (u64 k = 0; k < m; ++k) {
-    if (na[k] >= kDirectLimbs)
-      check_cuda(cudaMemcpyAsync(din + oa[k], P.a[k]->data, 8 * na[k], cudaMemcpyHostToDevice, st), "upload");
-    if (nb[k] >= kDirectLimbs)
-      check_cuda(cudaMemcpyAsync(din + ob[k], P.b[k]->data, 8 * nb[k], cudaMemcpyHostToDevice, st), "upload");
-  }
-  std::vector<nn_mul_job> jobs(m);
-  for (u64 k = 0; k < m; ++k) jobs[k] = nn_mul_job{din + oa[k], na[k], din + ob[k], nb[k], dout + oo[k]};
-  // long products land in fresh naturals, moved into place after the copies
-  // (an output may be one of the operands)
-  std::vector<std::unique_ptr<natural>> big(m);
-  nn_batch* B = nullptr;
-  nn_status s = nn_batch_create(c, na.data(), nb.data(), nullptr, m, &B);
-  if (s == NN_OK) s = nn_batch_launch(c, B, jobs.data());
-  if (s == NN_OK) {
-    if (tout_small)
-      check_cuda(cudaMemcpyAsync(hout, dout, 8 * tout_small, cudaMemcpyDeviceToHost, st), "download");
-    for (u64 k = 0; k < m; ++k)
-      if (na[k] + nb[k] >= kDirectLimbs) {
-        big[k] = std::make_unique<natural>();
-        big[k]->resize(na[k] + nb[k]);
-        check_cuda(cudaMemcpyAsync(big[k]->data, dout + oo[k], 8 * (na[k] + nb[k]), cudaMemcpyDeviceToHost, st),
-                   "download");
-      }
-  }
-  if (B) nn_batch_destroy(c, B);
-  cudaFreeAsync(din, st);
-  cudaFreeAsync(dout, st);
-  nn_gb300::check(s == NN_OK ? nn_context_synchronize(c) : s, "batched products");
-  parallel_for(m, 64, [&](u64 k) {
-    if (big[k])
-      *P.out[k] = std::move(big[k]->std());
-    else
-      *P.out[k] = to_natural(hout + oo[k], norm(hout + oo[k], na[k] + nb[k]));
-  });
-  S.gpu_s += since(t0);
-  S.gpu_products += m;
-  S.batches += 1;
-}
-
 // ---------------------------------------------------------------------------
 // Device-resident tree levels: the levels above the host subtrees keep their
 // values in device memory; each level's products go to the GPU as one batch
@@ -423,8 +323,9 @@ struct Event {  // a CUDA event for the duration of a scope
   }
 };
 
-// Sums out = x + y: short ones in one batched launch (one warp a sum), long
-// ones one multiword scan each.
+// Sums out = x + y (or differences x - y, x >= y): short ones in one batched
+// launch (one warp a sum), long ones one multiword scan each (a long
+// difference writes one limb past its nout).
 constexpr u64 kWarpAddLimbs = 1 << 15;
 void device_adds(nn_context* c, const std::vector<nn::AddJob>& jobs) {
   cudaStream_t st = (cudaStream_t)nn_context_stream(c);
@@ -434,7 +335,10 @@ void device_adds(nn_context* c, const std::vector<nn::AddJob>& jobs) {
       small.push_back(j);
       continue;
     }
-    check_cuda(nn::lin_combine(j.out, j.nout - 1, j.x, j.nx, 0, j.y, j.ny, 0, false, 0, nn::ctx_scan(c), st),
+    // a sum's carry goes to its top limb; a difference's (1: no borrow) to
+    // one limb past it, which its caller allocates
+    check_cuda(nn::lin_combine(j.out, j.sub ? j.nout : j.nout - 1, j.x, j.nx, 0, j.y, j.ny, 0, j.sub != 0,
+                               j.sub ? 1 : 0, nn::ctx_scan(c), st),
                "tree sum");
   }
   if (small.empty()) return;
@@ -856,13 +760,6 @@ void calc_e_levels(nn_context* c, u64 terms, natural& num, natural& den, u64 hos
 // Decimal output: _format_dec / _dec_split (natural.h:953-1011)
 // ---------------------------------------------------------------------------
 
-struct DecLevel {  // base[i] = 10^(18 * 2^i), its reciprocal and shift, as spans
-  const u64* base;
-  u64 nb;
-  const u64* base_r;
-  u64 nr;
-  u64 shift;  // ((base.size + 2) << 6) - n_shl
-};
 
 char* export_str(const std::string& s, u64* n) {
   *n = s.size();
@@ -874,111 +771,154 @@ char* export_str(const std::string& s, u64* n) {
   return p;
 }
 
+// A device copy of a host natural on the stream (the copy has read the
+// natural when this returns: pageable sources are staged at once, page-locked
+// ones are waited for).
+DNum to_device(DLevel& L, const natural& x) {
+  L.reserve(DLevel::words(x.size));
+  const DNum d = L.take(x.size);
+  check_cuda(cudaMemcpyAsync(d.p, x.data, 8 * x.size, cudaMemcpyHostToDevice, L.st), "upload");
+  check_cuda(cudaStreamSynchronize(L.st), "upload");
+  return d;
+}
+
+// A small host table into device memory freed with the level `L` (pageable
+// source: staged when the call returns).
+template <class T>
+const T* table(DLevel& L, const std::vector<T>& v) {
+  L.reserve((v.size() * sizeof(T) + 7) / 8);
+  check_cuda(cudaMemcpyAsync(L.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, L.st), "table");
+  return reinterpret_cast<const T*>(L.p);
+}
+
 // Decimal digits (std::formatter<natural>, natural.h:1089-1091) into a
 // malloc'd, NUL-terminated buffer of *len digits: the split tree of
-// _format_dec, level by level with GPU batches while the split powers are at
-// least host_below / 2 limbs; the nodes left are turned into digits on the
-// device, one thread a node (decimal.cu), and come back in one copy.
+// _format_dec, level by level while the split powers have at least
+// host_below limbs, all in device memory: a level's products (hi = base_r *
+// (v >> ..) >> shift, then base * hi) run as two batches, the shift as one
+// launch, lo = v - base * hi as one batched difference and the correction
+// loop (natural.h:962-965) as one launch, one warp a node; the nodes left
+// become digits on the device, one warp a node (decimal.cu), and the string
+// comes back in one copy.  Only node 0, the first, can end with hi = 0 and
+// then splits into its lo alone: one flag a level comes back for it.
 char* to_dec_levels(nn_context* c, const natural& x, u64 host_below, Staging& stg, Stats& S, u64* len) {
   using namespace nn_gb300;
+  (void)stg;
   const int top = dec_init(x);
   if (top < 0) return export_str(std::to_string(x[0]), len);
   DecCache& C = dec_cache();
-  std::vector<DecLevel> D(top + 1);
-  for (int i = 1; i <= top; ++i) {
-    const natural& b = C.base[i];
-    const unsigned n_shl = (unsigned)(std::countl_zero(b[b.size - 1]) + 1) & 63;
-    D[i] = DecLevel{b.data, b.size, C.base_r[i].data, C.base_r[i].size, ((b.size + 2) << 6) - n_shl};
-  }
-  struct Node {
-    natural v;
-    bool first;
-  };
-  std::vector<Node> lv;
-  lv.push_back(Node{x, true});
-  int i = top;
+  const auto t0 = Clock::now();
+  cudaStream_t st = (cudaStream_t)nn_context_stream(c);
   // Split levels while the split powers have at least host_below limbs: the
-  // device leaves below cost less than another batched level down to about
-  // there (measured on GB300, a 5 Mi-limb value to 10^8 digits: 0.192 s with
-  // levels down to 128 limbs, 0.167 s to 256, 0.181 s to 512)
-  // (at most 4000 limbs: the device leaves then stay within 8192 limbs a node)
+  // device leaves below cost less than another level down to about there
+  // (measured on GB300, a 5 Mi-limb value to 10^8 digits with the levels on
+  // host and device: 0.192 s with levels down to 128 limbs, 0.167 s to 256,
+  // 0.181 s to 512); at most 4000 limbs, so the leaves stay within 8192 limbs
+  // a node.
   const u64 dec_below = std::min<u64>(std::max<u64>(host_below, 16), 4000);
-  for (; i >= 1 && std::min(D[i].nb, D[i].nr) >= dec_below; --i) {
+  DLevel consts(st);  // a zero limb, the flags of a level and an error word
+  consts.reserve(4);
+  check_cuda(cudaMemsetAsync(consts.p, 0, 32, st), "constants");
+  const DNum zero1{consts.p, 1};
+  u32* err = reinterpret_cast<u32*>(consts.p + 2);
+  DLevel cur(st);
+  std::vector<DNum> nodes{to_device(cur, x)};
+  int i = top;
+  for (; i >= 1 && std::min(C.base[i].size, C.base_r[i].size) >= dec_below; --i) {
     const natural& base = C.base[i];
     const natural& base_r = C.base_r[i];
-    const u64 n = lv.size();
-    std::vector<natural> y(n), hi(n), lo(n), p(n);
-    parallel_for(n, 16, [&](u64 k) { y[k] = lv[k].v >> ((base.size - 1) << 6); });
-    Products P1;
+    const u64 nb = base.size, nr = base_r.size;
+    const unsigned n_shl = (unsigned)(std::countl_zero(base[nb - 1]) + 1) & 63;
+    const u64 shift = ((nb + 2) << 6) - n_shl;  // natural.h:958-960
+    DLevel bases(st), br(st);
+    const DNum dbase = to_device(bases, base), dbase_r = to_device(br, base_r);
+    const u64 n = nodes.size();
+    std::vector<DNum> y(n), hp(n), hi(n), p(n), lo(n);
+    u64 w = 0;
     for (u64 k = 0; k < n; ++k) {
-      if (y[k] == 0)
-        hi[k] = 0;
-      else
-        P1.add(&hi[k], &base_r, &y[k]);  // mul_load(hi, base_r, x >> .., ni)
+      const DNum v = nodes[k];
+      y[k] = v.n > nb - 1 ? DNum{v.p + nb - 1, v.n - (nb - 1)} : zero1;
+      const u64 nhp = nr + y[k].n, nhi = (nhp > (shift >> 6) ? nhp - (shift >> 6) : 1) + 1;
+      w += DLevel::words(nhp) + DLevel::words(nhi) + DLevel::words(nb + nhi) + DLevel::words(std::min(v.n, nb + 1) + 1);
     }
-    run_products(c, P1, stg, S);
-    parallel_for(n, 16, [&](u64 k) { hi[k] >>= D[i].shift; });
-    Products P2;
+    DLevel nxt(st);
+    nxt.reserve(w);
+    std::vector<nn_mul_job> j1(n), j2(n);
+    std::vector<nn::ShrJob> sh(n);
+    std::vector<nn::AddJob> sub(n);
+    std::vector<nn::DecFixJob> fix(n);
     for (u64 k = 0; k < n; ++k) {
-      if (hi[k] == 0)
-        p[k] = 0;
-      else
-        P2.add(&p[k], &base, &hi[k]);  // mul_load(lo, base, hi, ni)
+      const DNum v = nodes[k];
+      hp[k] = nxt.take(nr + y[k].n);
+      hi[k] = nxt.take((hp[k].n > (shift >> 6) ? hp[k].n - (shift >> 6) : 1) + 1);  // a limb for the corrections
+      p[k] = nxt.take(nb + hi[k].n);
+      // lo = v - base * hi is below a few times base (hi is at most a few
+      // short of the quotient), so nb + 1 limbs hold it and the difference is
+      // taken mod B^(nb+1); a long difference writes one limb past its length
+      const u64 nlo = std::min(v.n, nb + 1);
+      lo[k] = nxt.take(nlo + 1);
+      lo[k].n = nlo;
+      j1[k] = nn_mul_job{dbase_r.p, nr, y[k].p, y[k].n, hp[k].p};  // mul_load(hi, base_r, x >> .., ni)
+      sh[k] = nn::ShrJob{hp[k].p, hp[k].n, hi[k].p, hi[k].n, shift};
+      j2[k] = nn_mul_job{dbase.p, nb, hi[k].p, hi[k].n, p[k].p};  // mul_load(lo, base, hi, ni)
+      sub[k] = nn::AddJob{v.p, std::min(v.n, nlo), p[k].p, std::min(p[k].n, nlo), lo[k].p, nlo, 1};  // lo = *this - lo
+      fix[k] = nn::DecFixJob{lo[k].p, lo[k].n, hi[k].p, hi[k].n};
     }
-    run_products(c, P2, stg, S);
-    parallel_for(n, 16, [&](u64 k) {
-      lo[k] = lv[k].v - p[k];
-      while (lo[k] >= base) {  // natural.h:962-965
-        hi[k] += 1;
-        lo[k] -= base;
-      }
-    });
-    std::vector<Node> next;
+    std::vector<nn_batch*> plans;
+    struct Release {
+      nn_context* c;
+      std::vector<nn_batch*>& p;
+      ~Release() { release_plans(c, p); }
+    } release{c, plans};
+    plans.push_back(device_products(c, j1));
+    DLevel tsh(st), tfix(st), flags(st);
+    check_cuda(nn::shr_batch(table(tsh, sh), sh, st), "split shift");
+    plans.push_back(device_products(c, j2));
+    device_adds(c, sub);
+    flags.reserve((n + 1) / 2);
+    u32* zero = reinterpret_cast<u32*>(flags.p);
+    check_cuda(nn::dec_fix(table(tfix, fix), n, dbase.p, nb, zero, err, st), "split correction");
+    u32 hz[2] = {0, 0};  // node 0's hi == 0, the error word
+    check_cuda(cudaMemcpyAsync(&hz[0], zero, 4, cudaMemcpyDeviceToHost, st), "flag");
+    check_cuda(cudaMemcpyAsync(&hz[1], err, 4, cudaMemcpyDeviceToHost, st), "flag");
+    check_cuda(cudaStreamSynchronize(st), "split level");
+    if (hz[1]) throw std::runtime_error("natural_gb300: decimal split correction did not converge");
+    std::vector<DNum> next;
     next.reserve(2 * n);
     for (u64 k = 0; k < n; ++k) {
-      if (lv[k].first && hi[k] == 0) {
-        next.push_back(Node{std::move(lo[k]), true});
+      const DNum h{hi[k].p, std::min(hi[k].n, nb)}, l{lo[k].p, std::min(lo[k].n, nb)};  // both below base
+      if (k == 0 && hz[0]) {  // the first node with hi = 0 goes on as its lo (natural.h:1000-1003)
+        next.push_back(l);
       } else {
-        next.push_back(Node{std::move(hi[k]), lv[k].first});
-        next.push_back(Node{std::move(lo[k]), false});
+        next.push_back(h);
+        next.push_back(l);
       }
     }
-    lv.swap(next);
+    S.gpu_products += 2 * n;
+    nodes.swap(next);
+    cur = std::move(nxt);
   }
-  // The nodes left, each below base[i]^2 = 10^(18 * 2^(i+1)), on the device:
-  // node-major in one upload, 2^(i+1) groups of 18 digits a node written in
-  // place of the tree's leaves (natural.h:994-1011); node 0, the first, is
-  // written at the same width and loses its leading zeros on the way back.
-  const auto t0 = Clock::now();
-  const u64 n = lv.size();
+  // The nodes left, each below base[i]^2 = 10^(18 * 2^(i+1)): 2^(i+1) groups
+  // of 18 digits a node written in place of the tree's leaves
+  // (natural.h:994-1011); node 0, the first, is written at the same width and
+  // loses its leading zeros on the way back.
+  const u64 n = nodes.size();
   const u32 groups = 2u << i;
   const u64 width = 18ull * groups;
   u64 maxlen = 2;
-  for (const Node& nd : lv) maxlen = std::max(maxlen, span_len(nd.v));
-  const u64 stride = (maxlen + 1) & ~1ull;
-  const u64 words = stride * n + (n + 1) / 2;  // limbs, then the u32 lengths
-  u64* hw = stg.in.get(words);
-  u32* hlen = reinterpret_cast<u32*>(hw + stride * n);
-  parallel_for(n, 64, [&](u64 k) {
-    const u64 l = span_len(lv[k].v);
-    hlen[k] = (u32)l;
-    std::memcpy(hw + k * stride, lv[k].v.data, 8 * l);
-  });
-  cudaStream_t st = (cudaStream_t)nn_context_stream(c);
-  struct AsyncBuf {  // device buffer freed on the stream however the scope is left
-    cudaStream_t st;
-    void* p = nullptr;
-    ~AsyncBuf() {
-      if (p) cudaFreeAsync(p, st);
-    }
-  } bw{st}, bo{st};
-  check_cuda(cudaMallocAsync(&bw.p, 8 * words, st), "decimal nodes");
-  check_cuda(cudaMallocAsync(&bo.p, n * width, st), "decimal digits");
-  u64* dw = static_cast<u64*>(bw.p);
-  char* dout = static_cast<char*>(bo.p);
-  check_cuda(cudaMemcpyAsync(dw, hw, 8 * words, cudaMemcpyHostToDevice, st), "upload");
-  check_cuda(nn::dec_groups(dw, stride, reinterpret_cast<const u32*>(dw + stride * n), n, groups, dout, st),
-             "decimal kernel");
+  std::vector<const u64*> ptrs(n);
+  std::vector<u32> lens(n);
+  for (u64 k = 0; k < n; ++k) {
+    ptrs[k] = nodes[k].p;
+    lens[k] = (u32)nodes[k].n;
+    maxlen = std::max(maxlen, nodes[k].n);
+  }
+  DLevel tp(st), tl(st), bo(st);
+  const u64* const* dptrs = table(tp, ptrs);
+  const u32* dlens = table(tl, lens);
+  bo.reserve((n * width + 7) / 8);
+  char* dout = reinterpret_cast<char*>(bo.p);
+  check_cuda(nn::dec_groups(dptrs, (maxlen + 1) & ~1ull, dlens, n, groups, dout, st), "decimal kernel");
   std::string head(width, '0');
   check_cuda(cudaMemcpyAsync(head.data(), dout, width, cudaMemcpyDeviceToHost, st), "download");
   check_cuda(cudaStreamSynchronize(st), "decimal digits");
@@ -998,7 +938,6 @@ char* to_dec_levels(nn_context* c, const natural& x, u64 host_below, Staging& st
   S.gpu_s += since(t0);
   return out;
 }
-
 
 void fill_timing(double* t, const double* v, int k) {
   if (t)
