@@ -9,10 +9,11 @@
 //    limbs: millions of products of a few limbs) runs on host threads, one
 //    whole subtree per task, on flat limb spans in per-thread scratch (no
 //    allocation per node);
-//  - the levels above run level by level: every product of one level is
-//    independent, and the level's products go to the GPU as one batch
-//    (nn_batch_create/nn_batch_launch, the persistent work-queue kernel)
-//    through pinned staging buffers.
+//  - the levels above run level by level in device memory: every product of
+//    one level is independent, and the level's products go to the GPU as one
+//    batch (nn_batch_create/nn_batch_launch, the persistent work-queue
+//    kernel) on device pointers, its sums and differences as batched
+//    launches; values cross the host link once each way.
 // The values are the reference's: products are exact whichever way they are
 // computed, and the adds, |a - b| subtractions, shifts and correction loops
 // between them are the reference's own steps.
