@@ -263,19 +263,29 @@ def measure_series(ctx) -> dict:
     """pi and e to 10^8 digits (the reference's test.cpp recipes: pi with
     2^23 terms and a 6e6-limb square root, e with 2^24 terms), trees
     evaluated level by level with each level's products batched on the GPU;
-    the digit strings are compared with the reference's SHA-256 digests."""
+    the digit strings are compared with the reference's SHA-256 digests.
+    Each runs twice: the first call (page-locking host memory, growing the
+    twiddle tables) is reported as first_call_seconds, the second as
+    seconds."""
     import hashlib
     golden = json.load(open(os.path.join(ROOT, "tests", "golden", "golden.json")))
     out = {}
     for name in ("pi", "e"):
         c = golden["big_" + name][0]
+
+        def run():
+            if name == "pi":
+                return ctx.pi_dec_levels(c["terms"], c["acc"], c["digits"])
+            return ctx.e_dec_levels(c["terms"], c["digits"])
+
         t0 = time.perf_counter()
-        if name == "pi":
-            digits, timing = ctx.pi_dec_levels(c["terms"], c["acc"], c["digits"])
-        else:
-            digits, timing = ctx.e_dec_levels(c["terms"], c["digits"])
+        digits, _ = run()  # first call: page-locks host memory, grows tables
+        cold = time.perf_counter() - t0
+        del digits
+        t0 = time.perf_counter()
+        digits, timing = run()
         wall = time.perf_counter() - t0
-        out[name] = {"digits": c["digits"], "seconds": wall,
+        out[name] = {"digits": c["digits"], "seconds": wall, "first_call_seconds": cold,
                      "exact": hashlib.sha256(digits.encode()).hexdigest() == c["out"]["sha256"],
                      "reference_seconds_x86_1core": c.get("ref_seconds"),
                      "phases": {k: round(v, 3) for k, v in timing.items()}}

@@ -762,6 +762,18 @@ void calc_e_levels(nn_context* c, u64 terms, natural& num, natural& den, u64 hos
 // ---------------------------------------------------------------------------
 
 
+// a / b with every step of the division on the device (nn_divmod_host: the
+// quotient is unique, so it is natural::_div's); trivial and one-limb
+// divisors through the drop-in natural.
+natural div_on_device(nn_context* c, const natural& a, const natural& b) {
+  if (b.size == 1 || a < b) return a / b;
+  natural q, r;
+  q.resize(a.size - b.size + 1);
+  r.resize(b.size);
+  nn_gb300::check(nn_divmod_host(c, q.data, r.data, a.data, a.size, b.data, b.size), "division");
+  return std::move(q.std());
+}
+
 char* export_str(const std::string& s, u64* n) {
   *n = s.size();
   char* p = (char*)std::malloc(s.size() + 1);
@@ -964,7 +976,7 @@ nn_status nn_pi_dec_levels(nn_context* c, uint64_t terms, uint64_t acc, uint64_t
     num = 0xcf6371 * den - num;
     den *= 0x68380 * numc * pow(natural(10), digits);
     num *= denc;
-    den /= num;
+    den = div_on_device(c, den, num);
     const double t_div = since(t0) - t_tree;
     char* digits_out = to_dec_levels(c, den, host_below, stg, S, len);
     const double t_all = since(t0);
@@ -992,7 +1004,7 @@ nn_status nn_e_dec_levels(nn_context* c, uint64_t terms, uint64_t digits, uint64
     calc_e_levels(c, terms, num, den, host_below, stg, S);  // test.cpp:12-19 recipe
     const double t_tree = since(t0);
     num *= pow(natural(10), digits);
-    num /= den;
+    num = div_on_device(c, num, den);
     const double t_div = since(t0) - t_tree;
     char* digits_out = to_dec_levels(c, num, host_below, stg, S, len);
     const double t_all = since(t0);
