@@ -30,6 +30,99 @@ int ntt_scale(u64 n1, u64 n2) {  // get_NTT_scale (natural.h:384-386)
   u64 v = n1 + n2 - 2;
   return 64 - std::countl_zero(v);
 }
+
+// Page-locked staging ring for the small host tables a call uploads (batch
+// plans, job tables, sum tables).  A copy from pageable memory may wait for
+// the stream's earlier work before it returns, which would stop the host
+// from planning the next batch while the GPU runs this one; from this ring
+// the copy is queued and the call returns at once.  Regions are handed out
+// in order; one is reused after the event recorded behind its copy.
+struct Stager {
+  struct Region {
+    u64 off, len;
+    cudaEvent_t done;
+  };
+  char* base = nullptr;
+  u64 cap = 0, head = 0;
+  std::vector<Region> live;  // oldest first
+  std::vector<cudaEvent_t> spare;
+
+  void retire_front() {
+    spare.push_back(live.front().done);
+    live.erase(live.begin());
+  }
+  // Room for n bytes (256-byte granules), waiting for the copies that still
+  // read it; nullptr if no page-locked memory can be had.
+  char* reserve(u64 n) {
+    n = (n + 255) & ~255ull;
+    if (n > cap) {
+      while (!live.empty()) {
+        cudaEventSynchronize(live.front().done);
+        retire_front();
+      }
+      if (base) nn_host_free(base, cap);
+      cap = std::max<u64>(std::bit_ceil(2 * n), 16ull << 20);
+      base = static_cast<char*>(nn_host_alloc(cap));
+      head = 0;
+      if (!base) {
+        cap = 0;
+        return nullptr;
+      }
+    }
+    u64 off = head + n <= cap ? head : 0;
+    for (;;) {
+      while (!live.empty() && cudaEventQuery(live.front().done) == cudaSuccess) retire_front();
+      bool overlap = false;
+      for (const Region& r : live) overlap = overlap || (r.off < off + n && off < r.off + r.len);
+      if (!overlap) break;
+      cudaEventSynchronize(live.front().done);
+      retire_front();
+    }
+    head = off + n;
+    live.push_back(Region{off, n, nullptr});
+    return base + off;
+  }
+  // bytes from host memory at src to device memory at dst, queued on st.
+  cudaError_t upload(void* dst, const void* src, u64 bytes, cudaStream_t st) {
+    if (!bytes) return cudaSuccess;
+    char* h = reserve(bytes);
+    if (!h) return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);  // no page-locked memory
+    std::memcpy(h, src, bytes);
+    cudaError_t e = cudaMemcpyAsync(dst, h, bytes, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) {
+      live.pop_back();
+      return e;
+    }
+    if (spare.empty()) {
+      cudaEvent_t ev = nullptr;
+      e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+      if (e == cudaSuccess) spare.push_back(ev);
+    }
+    if (e == cudaSuccess) {
+      live.back().done = spare.back();
+      spare.pop_back();
+      e = cudaEventRecord(live.back().done, st);
+      if (e != cudaSuccess) spare.push_back(live.back().done);
+    }
+    if (e != cudaSuccess) {  // the copy is queued but no event marks its end: wait for it here
+      cudaStreamSynchronize(st);
+      live.pop_back();
+    }
+    return e;
+  }
+  void release() {
+    for (Region& r : live) {
+      cudaEventSynchronize(r.done);
+      cudaEventDestroy(r.done);
+    }
+    for (cudaEvent_t e : spare) cudaEventDestroy(e);
+    live.clear();
+    spare.clear();
+    if (base) nn_host_free(base, cap);
+    base = nullptr;
+    cap = head = 0;
+  }
+};
 }  // namespace
 
 struct nn_context {
@@ -47,6 +140,7 @@ struct nn_context {
   std::string err;
   u64* scratch[3] = {nullptr, nullptr, nullptr};  // grow-only device staging for host calls
   u64 scratch_words[3] = {0, 0, 0};
+  Stager stage;  // page-locked ring for uploaded tables
   // tunables (nn_context_set_tunable)
   int r_last = 11;            // levels of the contiguous NTT pass
   int r_col = 9;              // most levels of a strided column pass
@@ -635,10 +729,9 @@ nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, c
   B->d_state = reinterpret_cast<nn::u32*>(p + w_jobs + w_items + w_need);
   B->d_flags = reinterpret_cast<nn::u32*>(p + w_jobs + w_items + w_need + w_state);
   B->d_arena = p + w_jobs + w_items + w_need + w_state + w_flags;
-  NN_CK(c, cudaMemcpyAsync(B->d_items, B->items.data(), B->items.size() * sizeof(nn::BatchItem),
-                           cudaMemcpyHostToDevice, c->stream), "upload items");
-  NN_CK(c, cudaMemcpyAsync(B->d_need, B->need.data(), B->need.size() * 4, cudaMemcpyHostToDevice, c->stream),
-        "upload counts");
+  NN_CK(c, c->stage.upload(B->d_items, B->items.data(), B->items.size() * sizeof(nn::BatchItem), c->stream),
+        "upload items");
+  NN_CK(c, c->stage.upload(B->d_need, B->need.data(), B->need.size() * 4, c->stream), "upload counts");
   NN_CK(c, cudaEventCreateWithFlags(&B->ran, cudaEventDisableTiming), "event");
   return NN_OK;
 }
@@ -687,6 +780,9 @@ nn_status ctx_mul(nn_context* c, u64* out, const u64* a, u64 na, const u64* b, u
   return mul_impl(c, out, a, na, b, nb);
 }
 nn_status ctx_fail(nn_context* c, cudaError_t e, const char* what) { return fail(c, e, what); }
+cudaError_t ctx_upload(nn_context* c, void* d_dst, const void* h_src, u64 bytes) {
+  return c->stage.upload(d_dst, h_src, bytes, c->stream);
+}
 void ctx_error(nn_context* c, const char* msg) { c->err = msg; }
 nn_status ctx_scratch(nn_context* c, int slot, u64 words, u64** p) { return scratch(c, slot, words, p); }
 }  // namespace nn
@@ -824,6 +920,7 @@ nn_status nn_context_destroy(nn_context* c) {
   cudaStreamSynchronize(c->own);
   nn::tables_free(c->tables);
   nn::scan_free(c->scan);
+  c->stage.release();
   cudaStreamSynchronize(c->copy);
   cudaEventDestroy(c->ev_in);
   cudaEventDestroy(c->ev_chunk);
@@ -1138,14 +1235,12 @@ nn_status batch_fill(nn_context* c, nn_batch* B, const nn_mul_job* jobs, nn::Bat
 nn_status nn_batch_launch(nn_context* c, nn_batch* B, const nn_mul_job* jobs) {
   if (!c || !B || !jobs) return NN_ERR_INVALID;
   if (B->pending) NN_CK(c, cudaEventSynchronize(B->ran), "previous batch run");
-  // Pageable staging: the copy has taken the data when cudaMemcpyAsync returns,
-  // and no pinned allocation (which would synchronise the device) is needed.
+  // The table goes up through the context's page-locked ring: the call
+  // returns without waiting for the stream's earlier work.
   std::vector<nn::BatchJob> table(B->count);
   nn_status st = batch_fill(c, B, jobs, table.data());
   if (st != NN_OK) return st;
-  NN_CK(c, cudaMemcpyAsync(B->d_jobs, table.data(), B->count * sizeof(nn::BatchJob), cudaMemcpyHostToDevice,
-                           c->stream),
-        "upload jobs");
+  NN_CK(c, c->stage.upload(B->d_jobs, table.data(), B->count * sizeof(nn::BatchJob), c->stream), "upload jobs");
   NN_CK(c, cudaMemsetAsync(B->d_state, 0, (B->n_ctrs + 4) * 4, c->stream), "reset counters");
   NN_CK(c, cudaMemsetAsync(B->d_flags, 0, (B->n_flags + 2) * 4, c->stream), "reset flags");
   nn::launch_begin("batch_persistent", c->stream);

@@ -346,9 +346,7 @@ void device_adds(nn_context* c, const std::vector<nn::AddJob>& jobs) {
   DLevel tab(st);
   const u64 w = (small.size() * sizeof(nn::AddJob) + 7) / 8;
   tab.reserve(w);
-  // from pageable memory: the call returns once the table has been staged
-  check_cuda(cudaMemcpyAsync(tab.p, small.data(), small.size() * sizeof(nn::AddJob), cudaMemcpyHostToDevice, st),
-             "sum table");
+  check_cuda(nn::ctx_upload(c, tab.p, small.data(), small.size() * sizeof(nn::AddJob)), "sum table");
   check_cuda(nn::add_batch(reinterpret_cast<const nn::AddJob*>(tab.p), small.size(), st), "tree sums");
 }
 
@@ -795,12 +793,12 @@ DNum to_device(DLevel& L, const natural& x) {
   return d;
 }
 
-// A small host table into device memory freed with the level `L` (pageable
-// source: staged when the call returns).
+// A small host table into device memory freed with the level `L` (on the
+// context's stream, which is L's; v may change once this returns).
 template <class T>
-const T* table(DLevel& L, const std::vector<T>& v) {
+const T* table(nn_context* c, DLevel& L, const std::vector<T>& v) {
   L.reserve((v.size() * sizeof(T) + 7) / 8);
-  check_cuda(cudaMemcpyAsync(L.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, L.st), "table");
+  check_cuda(nn::ctx_upload(c, L.p, v.data(), v.size() * sizeof(T)), "table");
   return reinterpret_cast<const T*>(L.p);
 }
 
@@ -885,12 +883,12 @@ char* to_dec_levels(nn_context* c, const natural& x, u64 host_below, Staging& st
     } release{c, plans};
     plans.push_back(device_products(c, j1));
     DLevel tsh(st), tfix(st), flags(st);
-    check_cuda(nn::shr_batch(table(tsh, sh), sh, st), "split shift");
+    check_cuda(nn::shr_batch(table(c, tsh, sh), sh, st), "split shift");
     plans.push_back(device_products(c, j2));
     device_adds(c, sub);
     flags.reserve((n + 1) / 2);
     u32* zero = reinterpret_cast<u32*>(flags.p);
-    check_cuda(nn::dec_fix(table(tfix, fix), n, dbase.p, nb, zero, err, st), "split correction");
+    check_cuda(nn::dec_fix(table(c, tfix, fix), n, dbase.p, nb, zero, err, st), "split correction");
     u32 hz[2] = {0, 0};  // node 0's hi == 0, the error word
     check_cuda(cudaMemcpyAsync(&hz[0], zero, 4, cudaMemcpyDeviceToHost, st), "flag");
     check_cuda(cudaMemcpyAsync(&hz[1], err, 4, cudaMemcpyDeviceToHost, st), "flag");
@@ -927,8 +925,8 @@ char* to_dec_levels(nn_context* c, const natural& x, u64 host_below, Staging& st
     maxlen = std::max(maxlen, nodes[k].n);
   }
   DLevel tp(st), tl(st), bo(st);
-  const u64* const* dptrs = table(tp, ptrs);
-  const u32* dlens = table(tl, lens);
+  const u64* const* dptrs = table(c, tp, ptrs);
+  const u32* dlens = table(c, tl, lens);
   bo.reserve((n * width + 7) / 8);
   char* dout = reinterpret_cast<char*>(bo.p);
   check_cuda(nn::dec_groups(dptrs, (maxlen + 1) & ~1ull, dlens, n, groups, dout, st), "decimal kernel");

@@ -172,6 +172,10 @@ def test_mul_host_page_locked(ctx, oracle, na, nb):
     got = ctx.mul(pb, pa, out=po)  # shorter operand first
     assert np.array_equal(got, want)
     assert np.array_equal(ctx.mul(a, b), want)  # pageable
+    # operands one limb into their host buffers (8-byte aligned views)
+    va, vb = np.empty(na + 1, dtype=np.uint64), np.empty(nb + 1, dtype=np.uint64)
+    va[1:], vb[1:] = a, b
+    assert np.array_equal(ctx.mul(va[1:], vb[1:]), want)
 
 
 @pytest.mark.parametrize("na,nb", [(1 << 25, 1000), (1 << 25, 383), ((1 << 24) + 12345, (1 << 20) + 7),
