@@ -129,6 +129,8 @@ typedef struct nn_batch nn_batch;
  * others as three-prime NTT products at scale ceil(log2(n_a+n_b-1)).  All
  * pipelines go into one work queue drained by one persistent launch; the
  * launch sequence is captured in a CUDA graph on first run and replayed.
+ * Products at the "batch_solo_scale" tunable's scale and up run one at a
+ * time after that launch, as nn_mul (nn_sqr for squares) would.
  * square[j] (optional) marks squares. */
 nn_status nn_batch_create(nn_context* ctx, const uint64_t* n_a, const uint64_t* n_b, const int* square,
                           uint64_t count, nn_batch** out);
@@ -160,7 +162,10 @@ nn_status nn_batch_mul(nn_context* ctx, const nn_mul_job* jobs, uint64_t count);
  * tile; 0: tile by tile), "batch_split" (1, the default: an unbalanced
  * product may run as pieces of its longer operand, each through a smaller
  * transform sharing the shorter operand's, when that is estimated faster;
- * 0: one transform per product). */
+ * 0: one transform per product), "batch_solo_scale" (default 22: a batched
+ * product whose transform has this scale or more runs on its own through the
+ * one-product passes, after the batch kernel and before the run's completion;
+ * 0: every product in the batch kernel). */
 nn_status nn_context_set_tunable(nn_context* ctx, const char* name, int64_t value);
 int64_t nn_context_get_tunable(const nn_context* ctx, const char* name);
 
@@ -295,7 +300,8 @@ nn_status nn_e_dec_host(nn_context* ctx, uint64_t terms, uint64_t digits, char**
 /* The same recipes with the binary-splitting trees and the decimal split tree
  * evaluated level by level, each level's products as one GPU batch; the
  * series trees' bottom subtrees, whose values stay below about host_below
- * limbs (256 is a good choice), run whole on host threads.  The decimal split
+ * limbs (on a GB300 with 16 host cores: 128 for pi, 256 for e), run whole on
+ * host threads.  The decimal split
  * runs its levels while the split powers have at least host_below limbs;
  * the nodes left become digits on the device (one thread a node peels off
  * 18-digit groups, natural.h:566-573 and 994-1011) and come back in one copy.

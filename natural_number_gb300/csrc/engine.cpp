@@ -164,6 +164,7 @@ struct nn_context {
   int batch_merge = 1;        // batches: small tiles worked on 2048 words at a time
   int batch_split = 1;        // batches: unbalanced products in pieces sharing one transform
   int batch_blocks_per_sm = 0;  // persistent CTAs per SM (0: occupancy limit)
+  int batch_solo_scale = 22;    // batches: products of this scale and up run one at a time (0: never)
 };
 
 struct nn_batch {
@@ -174,6 +175,7 @@ struct nn_batch {
   std::vector<nn::u32> need;
   std::vector<u64> off_a, off_b;
   std::vector<char> swap;  // NTT job whose second operand is the longer one
+  std::vector<u64> solo;   // jobs run one at a time after the batch kernel
   u64 arena_words = 0;
   nn::u32 n_ctrs = 0, n_flags = 0;
   size_t smem = 0;
@@ -587,6 +589,14 @@ nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, c
       J.nb = std::min(na[j], nb[j]);
       J.piece = J.na;
       int s = ntt_scale(J.na, J.nb);
+      if (c->batch_solo_scale > 0 && s >= c->batch_solo_scale) {
+        // From this scale on the one-product passes (TMA tiles, fused last
+        // pass) beat the batch kernel's generic tiles (GB300, 4 products of
+        // 2^21 limbs: 4.65 ms against 5.55 ms), and one product already fills
+        // the GPU: no items, no arena; the launch runs it alone.
+        B->solo.push_back(j);
+        continue;
+      }
       if (c->batch_split && !J.square) s = batch_split(J.na, J.nb, s, &J.piece, &J.pieces);
       J.s = s;
       max_s = std::max(max_s, s);
@@ -638,7 +648,7 @@ nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, c
     B->n_ctrs += steps[j];
   }
   B->need.assign(B->n_ctrs, 0);
-  const int max_steps = *std::max_element(steps.begin(), steps.end());
+  const int max_steps = *std::max_element(steps.begin(), steps.end());  // 0 when every job runs alone
   B->items.clear();
   for (int st = 0; st < max_steps; ++st) {
     for (u64 j = 0; j < count; ++j) {
@@ -1169,6 +1179,8 @@ nn_status nn_context_set_tunable(nn_context* c, const char* name, int64_t v) {
     c->batch_split = (int)v;
   else if (k == "batch_blocks_per_sm" && v >= 0 && v <= 32)
     c->batch_blocks_per_sm = (int)v;
+  else if (k == "batch_solo_scale" && (v == 0 || (v >= 2 && v < 64)))
+    c->batch_solo_scale = (int)v;
   else {
     c->err = "unknown tunable or value out of range: " + k;
     return NN_ERR_INVALID;
@@ -1196,6 +1208,7 @@ int64_t nn_context_get_tunable(const nn_context* c, const char* name) {
   if (k == "batch_merge") return (int64_t)c->batch_merge;
   if (k == "batch_split") return (int64_t)c->batch_split;
   if (k == "batch_blocks_per_sm") return c->batch_blocks_per_sm;
+  if (k == "batch_solo_scale") return c->batch_solo_scale;
   return -1;
 }
 
@@ -1212,6 +1225,8 @@ nn_status nn_batch_create(nn_context* c, const uint64_t* na, const uint64_t* nb,
   *out = B;
   return NN_OK;
 }
+
+namespace {  // helpers of the batch entry points, not exported
 
 // Fills a job table (the plan's pinned one, or `into`) for one run.
 nn_status batch_fill(nn_context* c, nn_batch* B, const nn_mul_job* jobs, nn::BatchJob* into = nullptr) {
@@ -1232,6 +1247,19 @@ nn_status batch_fill(nn_context* c, nn_batch* B, const nn_mul_job* jobs, nn::Bat
   return NN_OK;
 }
 
+// The plan's large products, one at a time on the context's stream.
+nn_status batch_solo(nn_context* c, const nn_batch* B, const nn_mul_job* jobs) {
+  for (u64 j : B->solo) {
+    const nn_mul_job& m = jobs[j];
+    const nn_status st = B->jobs[j].square ? sqr_impl(c, m.d_out, m.d_a, m.n_a)
+                                           : mul_impl(c, m.d_out, m.d_a, m.n_a, m.d_b, m.n_b);
+    if (st != NN_OK) return st;
+  }
+  return NN_OK;
+}
+
+}  // namespace
+
 nn_status nn_batch_launch(nn_context* c, nn_batch* B, const nn_mul_job* jobs) {
   if (!c || !B || !jobs) return NN_ERR_INVALID;
   if (B->pending) NN_CK(c, cudaEventSynchronize(B->ran), "previous batch run");
@@ -1240,15 +1268,19 @@ nn_status nn_batch_launch(nn_context* c, nn_batch* B, const nn_mul_job* jobs) {
   std::vector<nn::BatchJob> table(B->count);
   nn_status st = batch_fill(c, B, jobs, table.data());
   if (st != NN_OK) return st;
-  NN_CK(c, c->stage.upload(B->d_jobs, table.data(), B->count * sizeof(nn::BatchJob), c->stream), "upload jobs");
-  NN_CK(c, cudaMemsetAsync(B->d_state, 0, (B->n_ctrs + 4) * 4, c->stream), "reset counters");
-  NN_CK(c, cudaMemsetAsync(B->d_flags, 0, (B->n_flags + 2) * 4, c->stream), "reset flags");
-  nn::launch_begin("batch_persistent", c->stream);
-  cudaError_t le = nn::batch_launch(B->d_jobs, B->d_items, (nn::u32)B->items.size(), B->d_need, B->d_state,
-                                    B->d_state + B->n_ctrs, B->d_flags, c->scan.err, c->tables, B->grid, B->smem,
-                                    c->stream);
-  nn::launch_end(c->stream);
-  NN_CK(c, le, "batch launch");
+  if (!B->items.empty()) {
+    NN_CK(c, c->stage.upload(B->d_jobs, table.data(), B->count * sizeof(nn::BatchJob), c->stream), "upload jobs");
+    NN_CK(c, cudaMemsetAsync(B->d_state, 0, (B->n_ctrs + 4) * 4, c->stream), "reset counters");
+    NN_CK(c, cudaMemsetAsync(B->d_flags, 0, (B->n_flags + 2) * 4, c->stream), "reset flags");
+    nn::launch_begin("batch_persistent", c->stream);
+    cudaError_t le = nn::batch_launch(B->d_jobs, B->d_items, (nn::u32)B->items.size(), B->d_need, B->d_state,
+                                      B->d_state + B->n_ctrs, B->d_flags, c->scan.err, c->tables, B->grid,
+                                      B->smem, c->stream);
+    nn::launch_end(c->stream);
+    NN_CK(c, le, "batch launch");
+  }
+  st = batch_solo(c, B, jobs);
+  if (st != NN_OK) return st;
   NN_CK(c, cudaEventRecord(B->ran, c->stream), "event record");
   B->pending = true;
   return NN_OK;
@@ -1262,14 +1294,18 @@ nn_status nn_batch_run(nn_context* c, nn_batch* B, const nn_mul_job* jobs) {
           "pinned jobs");
   nn_status fst = batch_fill(c, B, jobs);
   if (fst != NN_OK) return fst;
-  if (!B->exec) {
-    nn_status st = batch_capture(c, B);
-    if (st != NN_OK) return st;
+  if (!B->items.empty()) {
+    if (!B->exec) {
+      nn_status st = batch_capture(c, B);
+      if (st != NN_OK) return st;
+    }
+    nn::launch_begin("batch_persistent", c->stream);
+    cudaError_t ge = cudaGraphLaunch(B->exec, c->stream);
+    nn::launch_end(c->stream);
+    NN_CK(c, ge, "graph launch");
   }
-  nn::launch_begin("batch_persistent", c->stream);
-  cudaError_t ge = cudaGraphLaunch(B->exec, c->stream);
-  nn::launch_end(c->stream);
-  NN_CK(c, ge, "graph launch");
+  fst = batch_solo(c, B, jobs);
+  if (fst != NN_OK) return fst;
   NN_CK(c, cudaEventRecord(B->ran, c->stream), "event record");
   B->pending = true;
   return NN_OK;

@@ -173,3 +173,38 @@ def test_batch_tiny_transforms_with_largest_items(ctx, oracle):
             ctx.set_tunable(k, v)
     for k in range(len(sizes)):
         assert np.array_equal(normalize(outs[k]), oracle.mul(a_list[k], b_list[k])), k
+
+
+def test_batch_large_products_run_alone(ctx, oracle):
+    """Products at the batch_solo_scale tunable's scale (22: n_a + n_b - 1 >
+    2^21) run one at a time beside the batch kernel's items; the results equal
+    those of the batch kernel (batch_solo_scale 0) and, for the small ones and
+    a 2^20-limb square, the oracle's.  A plan of large products only launches
+    no batch kernel."""
+    sizes = [(1 << 21, 1 << 21), (300, 200), ((1 << 21) + 5, 1000), (5000, 7000), (1 << 20, 1 << 20),
+             ((1 << 20) + 1, (1 << 20) + 1)]
+    square = [0, 0, 0, 0, 1, 0]
+    a_list = [limbs(k + 31, x) for k, (x, _) in enumerate(sizes)]
+    b_list = [a if square[k] else limbs(k + 61, y) for k, ((_, y), a) in enumerate(zip(sizes, a_list))]
+    assert ctx.get_tunable("batch_solo_scale") == 22
+    outs, plan = run_batch(ctx, a_list, b_list, square=square)
+    old = ctx.get_tunable("batch_solo_scale")
+    try:
+        ctx.set_tunable("batch_solo_scale", 0)
+        ref, plan0 = run_batch(ctx, a_list, b_list, square=square)
+    finally:
+        ctx.set_tunable("batch_solo_scale", old)
+    assert plan.items < plan0.items
+    for k in range(len(sizes)):
+        assert np.array_equal(outs[k], ref[k]), k
+    for k in (1, 3):
+        assert np.array_equal(normalize(outs[k]), oracle.mul(a_list[k], b_list[k]))
+    assert np.array_equal(normalize(outs[4]), oracle.sqr(a_list[4]))
+    big = [0, 2, 5]
+    outs2, plan2 = run_batch(ctx, [a_list[k] for k in big], [b_list[k] for k in big])
+    assert plan2.items == 0
+    for j, k in enumerate(big):
+        assert np.array_equal(outs2[j], outs[k])
+    outs3, _ = run_batch(ctx, [a_list[k] for k in big], [b_list[k] for k in big], plan=plan2)  # replayed
+    for j, k in enumerate(big):
+        assert np.array_equal(outs3[j], outs[k])
