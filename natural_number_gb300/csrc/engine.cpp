@@ -1226,6 +1226,8 @@ nn_status nn_batch_create(nn_context* c, const uint64_t* na, const uint64_t* nb,
   return NN_OK;
 }
 
+}  // extern "C"
+
 namespace {  // helpers of the batch entry points, not exported
 
 // Fills a job table (the plan's pinned one, or `into`) for one run.
@@ -1259,6 +1261,8 @@ nn_status batch_solo(nn_context* c, const nn_batch* B, const nn_mul_job* jobs) {
 }
 
 }  // namespace
+
+extern "C" {
 
 nn_status nn_batch_launch(nn_context* c, nn_batch* B, const nn_mul_job* jobs) {
   if (!c || !B || !jobs) return NN_ERR_INVALID;
