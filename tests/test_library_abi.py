@@ -15,6 +15,22 @@ def test_library_exports_every_declared_symbol():
     assert not missing, missing
 
 
+def test_library_exports_nothing_else_with_c_linkage():
+    """Every unmangled function the library exports is one the header
+    declares: internal helpers keep internal linkage."""
+    import shutil
+    import subprocess
+    if not shutil.which("nm"):
+        pytest.skip("nm is not installed")
+    nn.lib()
+    out = subprocess.run(["nm", "-D", "--defined-only", nn.LIB_PATH], capture_output=True, text=True,
+                         check=True).stdout
+    exported = {f[2] for f in (line.split() for line in out.splitlines())
+                if len(f) == 3 and f[1] == "T" and not f[2].startswith("_Z")}
+    extra = sorted(exported - set(nn.header_functions()))
+    assert not extra, extra
+
+
 def test_status_strings():
     L = nn.lib()
     for s in range(7):
