@@ -213,10 +213,34 @@ __global__ void __launch_bounds__(256) dec_fix_kernel(const DecFixJob* __restric
     __syncwarp();
   }
   if (it == kMaxFix && lane == 0) atomicExch(err, 1u);
+  // hi == 0: the walk ends at the first nonzero limb (within the first 32
+  // limbs but for a zero or nearly zero hi)
   u32 nz = 0;
-  for (u64 i = lane; i < J.n_hi; i += 32) nz |= J.hi[i] != 0;
-  nz = __any_sync(0xffffffffu, nz);
+  for (u64 i0 = 0; i0 < J.n_hi && !nz; i0 += 32) {
+    const u64 i = i0 + lane;
+    nz = __any_sync(0xffffffffu, i < J.n_hi && J.hi[i] != 0);
+  }
   if (lane == 0) zero[k] = !nz;
+}
+
+__global__ void __launch_bounds__(256) dec_need_kernel(const DecFixJob* __restrict__ jobs, u64 m, const u64* base,
+                                                       u64 nb, u32* need) {
+  const u64 k = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const u32 lane = threadIdx.x & 31;
+  if (k >= m) return;  // whole warps leave together
+  const int c = warp_cmp(jobs[k].lo, jobs[k].n_lo, base, nb, lane);
+  if (lane == 0) need[k] = c >= 0;
+}
+
+// hi += 1 for the jobs with need[k] set, one warp a job (the walk stops once
+// no carry is left).
+__global__ void __launch_bounds__(256) dec_inc_kernel(const DecFixJob* __restrict__ jobs, u64 m,
+                                                      const u32* __restrict__ need) {
+  const u64 k = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const u32 lane = threadIdx.x & 31;
+  if (k >= m || !need[k]) return;  // whole warps leave together
+  const u64 one = 1;
+  warp_addsub(jobs[k].hi, jobs[k].n_hi, &one, 1, false, lane);
 }
 
 }  // namespace
@@ -265,6 +289,22 @@ cudaError_t shr_batch(const ShrJob* d_jobs, const std::vector<ShrJob>& jobs, cud
     shr_batch_kernel<<<dim3((unsigned)chunks, ny), 256, 0, st>>>(d_jobs + j0);
     launch_end(st);
   }
+  return cudaGetLastError();
+}
+
+cudaError_t dec_need(const DecFixJob* d_jobs, u64 m, const u64* base, u64 nb, u32* need, cudaStream_t st) {
+  if (m == 0) return cudaSuccess;
+  launch_begin("dec_need", st);
+  dec_need_kernel<<<(unsigned)((m * 32 + 255) / 256), 256, 0, st>>>(d_jobs, m, base, nb, need);
+  launch_end(st);
+  return cudaGetLastError();
+}
+
+cudaError_t dec_inc(const DecFixJob* d_jobs, u64 m, const u32* need, cudaStream_t st) {
+  if (m == 0) return cudaSuccess;
+  launch_begin("dec_inc", st);
+  dec_inc_kernel<<<(unsigned)((m * 32 + 255) / 256), 256, 0, st>>>(d_jobs, m, need);
+  launch_end(st);
   return cudaGetLastError();
 }
 

@@ -196,6 +196,11 @@ struct DecFixJob {
   u64 n_hi;
 };
 cudaError_t dec_fix(const DecFixJob* d_jobs, u64 m, const u64* base, u64 nb, u32* zero, u32* err, cudaStream_t st);
+// need[k] = (lo of job k >= base), one warp a job: the test of dec_fix's loop
+// alone, for callers that correct long nodes with multiword scans.
+cudaError_t dec_need(const DecFixJob* d_jobs, u64 m, const u64* base, u64 nb, u32* need, cudaStream_t st);
+// hi += 1 for the jobs with need[k] set, one warp a job.
+cudaError_t dec_inc(const DecFixJob* d_jobs, u64 m, const u32* need, cudaStream_t st);
 
 // Decimal digits of n short naturals at once (decimal.cu): node k's len[k]
 // limbs at nodes[k] (device pointers; len[k] <= stride, stride even and at

@@ -812,6 +812,44 @@ const T* table(nn_context* c, DLevel& L, const std::vector<T>& v) {
 // become digits on the device, one warp a node (decimal.cu), and the string
 // comes back in one copy.  Only node 0, the first, can end with hi = 0 and
 // then splits into its lo alone: one flag a level comes back for it.
+// The split's correction for a level of a few long nodes: dec_fix walks each
+// node with one warp, which for nodes of hundreds of thousands of limbs is a
+// long serial walk; here the test runs one warp a node, every subtraction
+// lo -= base is a multiword scan over the whole GPU (into `tmp`, then copied
+// back: a scan does not run in place), and hi += 1 one warp a node (the
+// walk stops once no carry is left).  Rounds end when no node has
+// lo >= base, after at most kMaxFixRounds (dec_fix, which runs next, then
+// reports any node still off).
+constexpr u64 kFixLoopNodes = 16, kFixLoopLimbs = 1 << 16;
+constexpr int kMaxFixRounds = 8;
+void fix_long_nodes(nn_context* c, const std::vector<nn::DecFixJob>& fix, const nn::DecFixJob* d_fix,
+                    const DNum& base, cudaStream_t st) {
+  const u64 n = fix.size();
+  u64 longest = 0;
+  for (const nn::DecFixJob& f : fix) longest = std::max(longest, f.n_lo);
+  DLevel tmp(st), flags(st);
+  tmp.reserve(longest + 2);
+  flags.reserve((n + 1) / 2);
+  u32* need = reinterpret_cast<u32*>(flags.p);
+  std::vector<u32> h_need(n);
+  for (int r = 0; r < kMaxFixRounds; ++r) {
+    check_cuda(nn::dec_need(d_fix, n, base.p, base.n, need, st), "split test");
+    check_cuda(cudaMemcpyAsync(h_need.data(), need, 4 * n, cudaMemcpyDeviceToHost, st), "split test");
+    check_cuda(cudaStreamSynchronize(st), "split test");
+    bool any = false;
+    for (u64 k = 0; k < n; ++k) {
+      if (!h_need[k]) continue;
+      any = true;
+      const nn::DecFixJob& f = fix[k];
+      check_cuda(nn::lin_combine(tmp.p, f.n_lo, f.lo, f.n_lo, 0, base.p, base.n, 0, true, 1, nn::ctx_scan(c), st),
+                 "split correction");
+      check_cuda(cudaMemcpyAsync(f.lo, tmp.p, 8 * f.n_lo, cudaMemcpyDeviceToDevice, st), "split correction");
+    }
+    if (!any) return;
+    check_cuda(nn::dec_inc(d_fix, n, need, st), "split correction");
+  }
+}
+
 char* to_dec_levels(nn_context* c, const natural& x, u64 host_below, Staging& stg, Stats& S, u64* len) {
   using namespace nn_gb300;
   (void)stg;
@@ -888,7 +926,9 @@ char* to_dec_levels(nn_context* c, const natural& x, u64 host_below, Staging& st
     device_adds(c, sub);
     flags.reserve((n + 1) / 2);
     u32* zero = reinterpret_cast<u32*>(flags.p);
-    check_cuda(nn::dec_fix(table(c, tfix, fix), n, dbase.p, nb, zero, err, st), "split correction");
+    const nn::DecFixJob* d_fix = table(c, tfix, fix);
+    if (n <= kFixLoopNodes && nb >= kFixLoopLimbs) fix_long_nodes(c, fix, d_fix, dbase, st);
+    check_cuda(nn::dec_fix(d_fix, n, dbase.p, nb, zero, err, st), "split correction");
     u32 hz[2] = {0, 0};  // node 0's hi == 0, the error word
     check_cuda(cudaMemcpyAsync(&hz[0], zero, 4, cudaMemcpyDeviceToHost, st), "flag");
     check_cuda(cudaMemcpyAsync(&hz[1], err, 4, cudaMemcpyDeviceToHost, st), "flag");

@@ -182,6 +182,24 @@ def test_to_dec_levels_edges_vs_python(ctx, host_below):
         sys.set_int_max_str_digits(old)
 
 
+def test_to_dec_levels_long_nodes_vs_recursive(ctx):
+    """Values of 2^17 to 2^18 limbs, whose top split levels have nodes of
+    2^16 limbs and more (corrected by multiword scans rather than one warp a
+    node): all-nines and powers of ten at a split power, and random limbs,
+    against the recursive conversion (natural's own to_string)."""
+    import sys
+    old = sys.get_int_max_str_digits()
+    sys.set_int_max_str_digits(0)
+    try:
+        e = 18 * 2 ** 18
+        vals = [10 ** e - 1, 10 ** e, 3 * 10 ** e - 1]
+        vals = [_limbs_of(v) for v in vals] + [limbs(4242, 1 << 18), limbs(4243, (1 << 17) + 12345)]
+        for x in vals:
+            assert ctx.to_dec_levels(x) == ctx.to_dec(x), x.size
+    finally:
+        sys.set_int_max_str_digits(old)
+
+
 @pytest.mark.parametrize("kind", ["pi", "e"])
 def test_levels_1e7_and_1e8_digits(ctx, golden, kind):
     """pi and e to 10^7 and 10^8 digits (the reference's recipes with 2^20 /
