@@ -252,15 +252,28 @@ __global__ void __launch_bounds__(256) add_batch_kernel(const AddJob* __restrict
   const AddJob J = jobs[j];
   const u64 flip = J.sub ? ~0ull : 0;
   u32 carry = J.sub ? 1 : 0;
-  for (u64 base = 0; base < J.nout; base += 32) {
-    const u64 k = base + lane;
-    const u64 a = k < J.nx ? J.x[k] : 0, b = (k < J.ny ? J.y[k] : 0) ^ flip;
-    const u64 sum = a + b;
-    const u32 G = __ballot_sync(0xffffffffu, sum < a), GP = __ballot_sync(0xffffffffu, sum < a || sum == ~0ull);
-    const u64 t = (u64)G + GP + carry;
-    const u32 cin = (((u32)t ^ G ^ GP) >> lane) & 1;
-    if (k < J.nout) J.out[k] = sum + cin;
-    carry = (u32)(t >> 32);
+  // four 32-limb steps' loads issued together, then their carries in order
+  constexpr int kSteps = 4;
+  for (u64 base = 0; base < J.nout; base += 32 * kSteps) {
+    u64 a[kSteps], b[kSteps];
+#pragma unroll
+    for (int q = 0; q < kSteps; ++q) {
+      const u64 k = base + 32 * q + lane;
+      a[q] = k < J.nx ? J.x[k] : 0;
+      b[q] = (k < J.ny ? J.y[k] : 0) ^ flip;
+    }
+#pragma unroll
+    for (int q = 0; q < kSteps; ++q) {
+      if (base + 32 * q >= J.nout) break;  // the same for every lane
+      const u64 k = base + 32 * q + lane;
+      const u64 sum = a[q] + b[q];
+      const u32 G = __ballot_sync(0xffffffffu, sum < a[q]),
+                GP = __ballot_sync(0xffffffffu, sum < a[q] || sum == ~0ull);
+      const u64 t = (u64)G + GP + carry;
+      const u32 cin = (((u32)t ^ G ^ GP) >> lane) & 1;
+      if (k < J.nout) J.out[k] = sum + cin;
+      carry = (u32)(t >> 32);
+    }
   }
 }
 
