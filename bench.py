@@ -13,7 +13,10 @@ CRT + carry into 2^28 product limbs.
   roofline  the dominant kernel's algorithmic bytes per launch over its mean
          event-timed duration, against the measured HBM copy bandwidth.
   cpu_baseline  the oracle (CPU restatement of the reference, 1 thread) on a
-         bounded sample: one 2^24 x 2^24-limb product.
+         bounded sample: one 2^24 x 2^24-limb product.  The batched and
+         served workloads carry their own cpu_baseline: the oracle on every
+         host core, one job a process (all 4096 products; a stratified
+         sample of the served stream).
 
 Inputs (2 GiB operands, 6 GiB of residues per transform) are far larger than
 the 129 MB L2, so no flush is needed between steps.  Multi-GPU runs are
@@ -318,6 +321,88 @@ def _ref_worker(args):
 
 REF_N_EXP = 23
 
+# Pooled CPU baselines of the batched and served workloads: every host core
+# runs the oracle restatement (the reference's algorithm, one job at a time,
+# as the reference would in one process per core); workers rebuild operands
+# from their seeds instead of receiving them through pipes.
+_POOL_STATE: dict = {}
+
+
+def _pool_init(serve_seed: int, serve_hi: float) -> None:
+    from oracle import Oracle
+    _POOL_STATE["oracle"] = Oracle("port")
+    if serve_seed >= 0:
+        from natural_number_gb300.synth import limbs
+        _POOL_STATE["pool"] = limbs(serve_seed, (1 << int(serve_hi + 0.999)) * 2 + 64)
+
+
+def _pool_job(task) -> float:
+    """One product (from seeds, or slices of the served pool) or one division."""
+    o = _POOL_STATE["oracle"]
+    kind = task[0]
+    if kind == "seeded":
+        from natural_number_gb300.synth import limbs
+        _, sa, na, sb, nb = task
+        a, b = limbs(sa, na), limbs(sb, nb)
+    else:
+        _, oa, na, ob, nb = task
+        pool = _POOL_STATE["pool"]
+        a, b = pool[oa:oa + na], pool[ob:ob + nb]
+    t0 = time.perf_counter()
+    if kind == "div":
+        o.div(a, b)
+    else:
+        o.mul(a, b)
+    return time.perf_counter() - t0
+
+
+def _pooled(tasks, serve_seed: int = -1, serve_hi: float = 0) -> tuple[float, int]:
+    import multiprocessing as mp
+    from oracle import build_oracle
+    build_oracle()
+    cores = os.cpu_count() or 1
+    with mp.get_context("spawn").Pool(cores, initializer=_pool_init, initargs=(serve_seed, serve_hi)) as pool:
+        t0 = time.perf_counter()
+        pool.map(_pool_job, tasks, chunksize=1)
+        return time.perf_counter() - t0, cores
+
+
+def cpu_baseline_batched(count: int) -> dict:
+    """All `count` products of the uneven batch, spread over the host cores."""
+    import numpy as np
+
+    from natural_number_gb300.synth import log_uniform_sizes
+    seed = 3  # UnevenProducts' default
+    sa = np.maximum(log_uniform_sizes(seed, count, 6, 18).astype(np.int64), 1)
+    sb = np.maximum(log_uniform_sizes(seed + 1, count, 6, 18).astype(np.int64), 1)
+    tasks = [("seeded", seed * 1000003 + 2 * j, int(sa[j]), seed * 1000003 + 2 * j + 1, int(sb[j]))
+             for j in range(count)]
+    tasks.sort(key=lambda t: -(t[2] + t[4]))  # longest first: the pool's tail stays short
+    dt, cores = _pooled(tasks)
+    total = int((sa + sb).sum())
+    return {"value": total / dt, "unit": UNIT, "cores": cores, "kind": "port", "seconds": dt,
+            "sample": "all %d products, one process a core, each product alone" % count}
+
+
+def cpu_baseline_serving(jobs: int, every: int = 20) -> dict:
+    """A stratified sample of the served stream (every `every`-th job, in
+    submission order) spread over the host cores; the whole stream takes
+    minutes on the CPU."""
+    from natural_number_gb300.serving import ServeWorkload
+    W = ServeWorkload(jobs)
+    base = W.pool.ctypes.data
+    tasks, total = [], 0
+    for k in range(0, len(W.jobs), every):
+        kind, a, b, units = W.jobs[k]
+        oa, ob = (a.ctypes.data - base) // 8, (b.ctypes.data - base) // 8
+        tasks.append((kind, int(oa), int(a.size), int(ob), int(b.size)))
+        total += units
+    tasks.sort(key=lambda t: -(t[2] + t[4]))
+    dt, cores = _pooled(tasks, serve_seed=9, serve_hi=22)
+    return {"value": total / dt, "unit": UNIT, "cores": cores, "kind": "port", "seconds": dt,
+            "sample": "%d of %d jobs (every %d-th, %d divisions), one process a core"
+                      % (len(tasks), len(W.jobs), every, sum(t[0] == "div" for t in tasks))}
+
 
 def run_reference(args) -> None:
     """CPU reference arm: the oracle restatement (the reference's x86-64
@@ -598,12 +683,20 @@ def main() -> None:
         r = legs.run("batched", 240, lambda: measure_batched(ctx, args.steps, args.warmup, args.batch_count))
         if r:
             line["batched"] = r
+            if rank == 0 and not args.no_cpu:
+                c = legs.run("cpu_baseline_batched", 240, lambda: cpu_baseline_batched(args.batch_count))
+                if c:
+                    r["cpu_baseline"] = c
     if rank == 0 and not args.no_serve:
         from natural_number_gb300 import serving as serving_mod
         rates = tuple(float(x) for x in args.serve_rates.split(",") if x)
         r = legs.run("serving", 420, lambda: serving_mod.measure(args.serve_jobs, rates))
         if r:
             line["serving"] = r
+            if not args.no_cpu:
+                c = legs.run("cpu_baseline_serving", 240, lambda: cpu_baseline_serving(args.serve_jobs))
+                if c:
+                    r["cpu_baseline"] = c
     if rank == 0 and not args.no_series:
         r = legs.run("series", 240, lambda: measure_series(ctx))
         if r:

@@ -309,7 +309,7 @@ class Context:
     def pi_dec_levels(self, terms: int, acc: int, digits: int, host_below: int = 128):
         """pi digits with level-by-level batched trees; returns (digits, timing dict).
         host_below 128 balances the host subtrees against the device levels on
-        a GB300 with 16 host cores (pi to 10^8 digits: 0.48 s, 0.59 s at 256)."""
+        a GB300 with 16 host cores (pi to 10^8 digits: 0.46 s, 0.59 s at 256)."""
         p, n, t = _vp(), C.c_uint64(), (C.c_double * 8)()
         self._check(lib().nn_pi_dec_levels(self.h, terms, acc, digits, host_below, C.byref(p), C.byref(n), t),
                     "pi_dec_levels")
