@@ -190,7 +190,8 @@ def measure_batched(ctx, steps: int, warmup: int, count: int = 4096) -> dict:
     identical = bool(torch.equal(W.out_plain, W.out_batch))
     out = {"workload": "%d products, operand lengths log-uniform in [2^6, 2^18] limbs (independent), "
                        "%d product limbs in total, %.0f%% of products on the NTT route"
-                       % (count, W.limbs_total, 100 * W.ntt_fraction(ctx.get_tunable("batch_ntt_min"))),
+                       % (count, W.limbs_total, 100 * W.ntt_fraction(ctx.get_tunable("batch_ntt_min"),
+                                                                      ctx.get_tunable("batch_school_balanced"))),
            "plain_ms": plain_ms, "batched_ms": batch_ms,
            "plain_limbs_per_s": W.limbs_total / (plain_ms / 1e3),
            "batched_limbs_per_s": W.limbs_total / (batch_ms / 1e3),

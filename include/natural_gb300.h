@@ -126,7 +126,8 @@ typedef struct nn_batch nn_batch;
 /* Plans a batch for these operand sizes (the reference has no batch API;
  * each job is natural::_mul, natural.h:444-450): jobs whose shorter operand
  * is below the "batch_ntt_min" tunable run as schoolbook column scans, the
- * others as three-prime NTT products at scale ceil(log2(n_a+n_b-1)).  All
+ * others (but balanced ones below "batch_school_balanced") as three-prime
+ * NTT products at scale ceil(log2(n_a+n_b-1)).  All
  * pipelines go into one work queue drained by one persistent launch; the
  * launch sequence is captured in a CUDA graph on first run and replayed.
  * Products at the "batch_solo_scale" tunable's scale and up run one at a
@@ -152,7 +153,10 @@ nn_status nn_batch_mul(nn_context* ctx, const nn_mul_job* jobs, uint64_t count);
  * "r_col@<s>" (the same for transforms of scale s only; 0 = default),
  * "batch_r_last@<s>" (r_last for batched transforms of scale s; 0 = as for
  * one product),
- * "batch_ntt_min" (default 384), "batch_blocks_per_sm" (0 = occupancy limit),
+ * "batch_ntt_min" (default 384), "batch_school_balanced" (default 256: a
+ * product whose longer operand is at most twice its shorter also takes the
+ * schoolbook route while the shorter is below this; 0 = off),
+ * "batch_blocks_per_sm" (0 = occupancy limit),
  * "batch_item_words" (residues per prime a batch pass item covers at least,
  * in consecutive tiles; default 8192), "batch_fused" (1, the default: a
  * batched transform of two passes or more runs the second operand's last

@@ -51,6 +51,63 @@ __device__ __forceinline__ void wide_tile(int C, u64* sm, const u64* in, u64* ou
     pass_tile<128, !INV, INV, INV, true>(sm, in, out, n_in, s, l0, R, tab, t.cap, prime, tile);
 }
 
+// A base-case item: the column sums of one scan tile's positions and of the
+// kScanE positions before them (the scan reads those too), all 256 threads
+// at once, eight lanes a position, into shared memory as three word arrays
+// of kColumnTileWords; the scan then reads them from there.  (With one
+// thread computing its scan positions' sums in turn, a product of a few
+// hundred limbs kept a few dozen threads of the CTA busy.)
+struct SmemSumsProducer {
+  static constexpr bool kBulk = true;
+  const u64* s;
+  u64 first;  // the position at s[0] (mod 2^64: tile 0's is -kScanE)
+  u64 total;
+  __device__ __forceinline__ W3 operator()(u64 k) const {
+    if (k >= total) return W3{0, 0, 0};
+    const u64 i = k - first;
+    return W3{s[i], s[kColumnTileWords + i], s[2 * kColumnTileWords + i]};
+  }
+  __device__ __forceinline__ void bulk(u64 k0, W3 (&x)[kScanE]) const {
+#pragma unroll
+    for (int e = 0; e < kScanE; ++e) x[e] = (*this)(k0 + e);
+  }
+};
+
+__device__ __forceinline__ void column_tile_sums(u64* sm, const BatchJob& J, u64 tile) {
+  constexpr u32 kLanes = 8, kGroups = 256 / kLanes;
+  const u64 size = J.na + J.nb;
+  const long long first = (long long)(tile * kScanTile) - kScanE;
+  const u64 end = min(size, (tile + 1) * kScanTile);
+  const u32 npos = (u32)((long long)end - first);  // at most kColumnTileWords
+  const u32 g = threadIdx.x / kLanes, j = threadIdx.x % kLanes;
+  const u32 rounds = (npos + kGroups - 1) / kGroups;  // the same for every thread
+  for (u32 r = 0; r < rounds; ++r) {
+    const u32 q = r * kGroups + g;
+    const long long p = first + q;
+    W3 acc{0, 0, 0};
+    if (q < npos && p >= 0 && (u64)p + 1 < size) {
+      const u64 k = (u64)p;
+      const u64 lo = k >= J.nb ? k - J.nb + 1 : 0;
+      const u64 hi = k < J.na - 1 ? k : J.na - 1;
+      for (u64 i = lo + j; i <= hi; i += kLanes) {
+        const u64 x = J.a[i], y = J.b[k - i];
+        acc = add_w3(acc, W3{x * y, mulhi(x, y), 0});
+      }
+    }
+#pragma unroll
+    for (u32 d = kLanes / 2; d >= 1; d >>= 1) {  // every lane of the warp takes part
+      const W3 o{__shfl_down_sync(0xffffffffu, acc.w0, d, kLanes), __shfl_down_sync(0xffffffffu, acc.w1, d, kLanes),
+                 __shfl_down_sync(0xffffffffu, acc.w2, d, kLanes)};
+      acc = add_w3(acc, o);
+    }
+    if (j == 0 && q < npos) {
+      sm[q] = acc.w0;
+      sm[kColumnTileWords + q] = acc.w1;
+      sm[2 * kColumnTileWords + q] = acc.w2;
+    }
+  }
+}
+
 // The transform that tile g of a pass over the first operand's pieces
 // belongs to, and the tile's index within it.
 struct PieceTile {
@@ -196,7 +253,9 @@ __global__ void __launch_bounds__(256, 3) batch_kernel(const BatchJob* __restric
       }
       case kItemColumn: {
         const u64 size = J.na + J.nb;
-        ColumnProducer prod{J.a, J.na, J.b, J.nb};
+        column_tile_sums(sm, J, it.tile);
+        __syncthreads();
+        const SmemSumsProducer prod{sm, (u64)it.tile * kScanTile - kScanE, size};
         scan_tile(prod, it.tile, size, J.out, size, nullptr, flags + J.flag_base, err);
         break;
       }

@@ -159,6 +159,7 @@ struct nn_context {
     return nn::plan_passes(s, batch_r_last_at[s], r_col_at[s] ? r_col_at[s] : r_col);
   }
   u64 batch_ntt_min = 384;    // batches: schoolbook when min(n_a, n_b) is below this
+  u64 batch_school_balanced = 256;  // ... or below this when max(n_a, n_b) <= 2 min(n_a, n_b) (0: off)
   u64 batch_item_words = nn::kBatchItemWords;  // residues a pass item covers at least
   int batch_fused = 1;        // batches: fused last pass (forward + pointwise + inverse)
   int batch_merge = 1;        // batches: small tiles worked on 2048 words at a time
@@ -574,9 +575,11 @@ nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, c
     J.ctr_base = B->n_ctrs;
     J.flag_base = B->n_flags;
     B->n_flags += (nn::u32)nn::scan_tiles(na[j] + nb[j]);
-    if (std::min(na[j], nb[j]) < c->batch_ntt_min) {
+    const u64 mn = std::min(na[j], nb[j]), mx = std::max(na[j], nb[j]);
+    if (mn < c->batch_ntt_min || (mn < c->batch_school_balanced && mx <= 2 * mn)) {
       J.s = 0;
       steps[j] = 1;
+      smem = std::max(smem, nn::kColumnTileSmem);  // the item's column sums
     } else {
       J.square = square ? square[j] : 0;
       if (J.square && na[j] != nb[j]) {
@@ -1181,6 +1184,8 @@ nn_status nn_context_set_tunable(nn_context* c, const char* name, int64_t v) {
     c->batch_blocks_per_sm = (int)v;
   else if (k == "batch_solo_scale" && (v == 0 || (v >= 2 && v < 64)))
     c->batch_solo_scale = (int)v;
+  else if (k == "batch_school_balanced" && v >= 0)
+    c->batch_school_balanced = (u64)v;
   else {
     c->err = "unknown tunable or value out of range: " + k;
     return NN_ERR_INVALID;
@@ -1209,6 +1214,7 @@ int64_t nn_context_get_tunable(const nn_context* c, const char* name) {
   if (k == "batch_split") return (int64_t)c->batch_split;
   if (k == "batch_blocks_per_sm") return c->batch_blocks_per_sm;
   if (k == "batch_solo_scale") return c->batch_solo_scale;
+  if (k == "batch_school_balanced") return (int64_t)c->batch_school_balanced;
   return -1;
 }
 

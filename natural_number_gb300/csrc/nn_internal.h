@@ -61,6 +61,10 @@ struct Scan {
 constexpr int kScanThreads = 256;
 constexpr int kScanE = 8;  // limbs per thread
 constexpr u64 kScanTile = (u64)kScanThreads * kScanE;
+// A batched base-case item's column sums in shared memory: a scan tile's
+// positions and the kScanE before them, three words each.
+constexpr u64 kColumnTileWords = kScanTile + kScanE;
+constexpr size_t kColumnTileSmem = 3 * kColumnTileWords * 8;
 
 // Batched products (batch.cu): jobs, their work items, and the launch.  A
 // pass item covers consecutive tiles worth at least kBatchItemWords residues

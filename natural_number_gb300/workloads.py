@@ -55,5 +55,10 @@ class UnevenProducts:
         t = self.out_batch if which == "batch" else self.out_plain
         return t[int(oo[j]):int(oo[j + 1])].cpu().numpy()
 
-    def ntt_fraction(self, threshold: int = 384) -> float:
-        return float(np.mean(np.minimum(self.sa, self.sb) >= threshold))
+    def ntt_fraction(self, threshold: int = 384, balanced: int = 0) -> float:
+        """Share of products a batch sends down the NTT route: the shorter
+        operand at least `threshold` limbs, and at least `balanced` when the
+        longer is at most twice the shorter."""
+        mn, mx = np.minimum(self.sa, self.sb), np.maximum(self.sa, self.sb)
+        school = (mn < threshold) | ((mn < balanced) & (mx <= 2 * mn))
+        return float(np.mean(~school))

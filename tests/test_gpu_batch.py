@@ -64,16 +64,18 @@ def test_batch_squares_and_threshold_tunable(ctx, oracle):
     outs, _ = run_batch(ctx, a_list, a_list, square=[1] * len(sizes))
     for k, a in enumerate(a_list):
         assert np.array_equal(normalize(outs[k]), oracle.sqr(a))
-    old = ctx.get_tunable("batch_ntt_min")
+    old = {k: ctx.get_tunable(k) for k in ("batch_ntt_min", "batch_school_balanced")}
     try:
         ctx.set_tunable("batch_ntt_min", 64)  # push mid sizes onto the NTT route
+        ctx.set_tunable("batch_school_balanced", 0)
         a_list = [limbs(k + 70, x) for k, x in enumerate([64, 100, 200, 383])]
         b_list = [limbs(k + 80, x) for k, x in enumerate([70, 100, 250, 383])]
         outs, _ = run_batch(ctx, a_list, b_list)
         for k in range(4):
             assert np.array_equal(normalize(outs[k]), oracle.mul(a_list[k], b_list[k]))
     finally:
-        ctx.set_tunable("batch_ntt_min", old)
+        for k, v in old.items():
+            ctx.set_tunable(k, v)
 
 
 def test_batch_fused_last_pass_matches_unfused(ctx, oracle):
@@ -163,9 +165,10 @@ def test_batch_tiny_transforms_with_largest_items(ctx, oracle):
     sizes = [(1, 1), (2, 3), (5, 5), (9, 7), (33, 31), (130, 2), (1000, 1000)]
     a_list = [limbs(k + 901, x) for k, (x, _) in enumerate(sizes)]
     b_list = [limbs(k + 951, y) for k, (_, y) in enumerate(sizes)]
-    old = {k: ctx.get_tunable(k) for k in ("batch_ntt_min", "batch_item_words")}
+    old = {k: ctx.get_tunable(k) for k in ("batch_ntt_min", "batch_item_words", "batch_school_balanced")}
     try:
         ctx.set_tunable("batch_ntt_min", 1)
+        ctx.set_tunable("batch_school_balanced", 0)
         ctx.set_tunable("batch_item_words", 1 << 20)
         outs, _ = run_batch(ctx, a_list, b_list)
     finally:
@@ -208,3 +211,28 @@ def test_batch_large_products_run_alone(ctx, oracle):
     outs3, _ = run_batch(ctx, [a_list[k] for k in big], [b_list[k] for k in big], plan=plan2)  # replayed
     for j, k in enumerate(big):
         assert np.array_equal(outs3[j], outs[k])
+
+
+def test_batch_base_case_items_vs_oracle(ctx, oracle):
+    """Every product on the base-case route (batch_ntt_min above all sizes):
+    single-tile and multi-tile column scans (up to 7000 positions, so tiles
+    whose sums start kScanE positions before them), one-limb operands,
+    all-ones limbs (the largest column sums) and squares, against the oracle."""
+    sizes = [(1, 1), (1, 7), (2, 2), (33, 1), (100, 80), (383, 383), (1000, 1048), (1025, 1024), (3000, 2000),
+             (5000, 2000), (2047, 1), (1, 2049)]
+    a_list = [limbs(k + 301, x) for k, (x, _) in enumerate(sizes)]
+    b_list = [limbs(k + 401, y) for k, (_, y) in enumerate(sizes)]
+    a_list.append(np.full(1500, 2**64 - 1, dtype=np.uint64))
+    b_list.append(np.full(1400, 2**64 - 1, dtype=np.uint64))
+    old = ctx.get_tunable("batch_ntt_min")
+    try:
+        ctx.set_tunable("batch_ntt_min", 1 << 20)
+        outs, _ = run_batch(ctx, a_list, b_list)
+        for k in range(len(a_list)):
+            assert np.array_equal(normalize(outs[k]), normalize(oracle.mul(a_list[k], b_list[k]))), k
+        sq = [limbs(k + 501, x) for k, x in enumerate([1, 5, 700, 2500])]
+        outs, _ = run_batch(ctx, sq, sq, square=[1] * len(sq))
+        for k, a in enumerate(sq):
+            assert np.array_equal(normalize(outs[k]), normalize(oracle.sqr(a))), k
+    finally:
+        ctx.set_tunable("batch_ntt_min", old)
