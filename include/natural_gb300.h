@@ -169,7 +169,9 @@ nn_status nn_batch_mul(nn_context* ctx, const nn_mul_job* jobs, uint64_t count);
  * 0: one transform per product), "batch_solo_scale" (default 22: a batched
  * product whose transform has this scale or more runs on its own through the
  * one-product passes, after the batch kernel and before the run's completion;
- * 0: every product in the batch kernel). */
+ * 0: every product in the batch kernel; runs that overlap on different
+ * streams of one context need 0, since those passes share the context's
+ * carry-scan scratch, as nn_mul calls on two streams do). */
 nn_status nn_context_set_tunable(nn_context* ctx, const char* name, int64_t value);
 int64_t nn_context_get_tunable(const nn_context* ctx, const char* name);
 

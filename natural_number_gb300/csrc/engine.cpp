@@ -141,6 +141,10 @@ struct nn_context {
   u64* scratch[3] = {nullptr, nullptr, nullptr};  // grow-only device staging for host calls
   u64 scratch_words[3] = {0, 0, 0};
   Stager stage;  // page-locked ring for uploaded tables
+  // Twiddle tables replaced by larger ones: kept until the context goes, as
+  // work on another stream (set_stream, or a server's concurrent batches)
+  // may still read them; together at most the size of the live tables.
+  std::vector<u64*> retired_tables;
   // tunables (nn_context_set_tunable)
   int r_last = 11;            // levels of the contiguous NTT pass
   int r_col = 9;              // most levels of a strided column pass
@@ -265,7 +269,7 @@ nn_status forward(nn_context* c, nn_transform* t, const u64* d_limbs, u64 n, int
     c->err = "forward: need 2 <= scale <= 40 and 1 <= n <= 2^scale";
     return NN_ERR_INVALID;
   }
-  NN_CK(c, nn::tables_ensure(c->tables, s, c->stream), "twiddle tables");
+  NN_CK(c, nn::tables_ensure(c->tables, s, c->stream, &c->retired_tables), "twiddle tables");
   nn_status st = xform_reserve(c, t, s);
   if (st != NN_OK) return st;
   const std::vector<nn::Pass> plan = c->passes(s);
@@ -321,7 +325,7 @@ nn_status pointwise(nn_context* c, nn_transform* dst, const nn_transform* a, con
 // with the pointwise product by `other` (nullptr: square) and the first
 // inverse pass; the caller finishes with inverse_save(skip_last_pass).
 nn_status forward_fused(nn_context* c, nn_transform* t, const u64* d_limbs, u64 n, int s, const nn_transform* other) {
-  NN_CK(c, nn::tables_ensure(c->tables, s, c->stream), "twiddle tables");
+  NN_CK(c, nn::tables_ensure(c->tables, s, c->stream, &c->retired_tables), "twiddle tables");
   nn_status st = xform_reserve(c, t, s);
   if (st != NN_OK) return st;
   const std::vector<nn::Pass> plan = c->passes(s);
@@ -378,7 +382,7 @@ nn_status ntt_product_from_host(nn_context* c, u64* d_out, u64* da, const u64* h
   u64 tiles = 0;
   if (plan.size() < 2 || !nn::ntt_first_pass_tiles(s, plan[0], &tiles)) return NN_OK;
   *used = true;
-  NN_CK(c, nn::tables_ensure(c->tables, s, c->stream), "twiddle tables");
+  NN_CK(c, nn::tables_ensure(c->tables, s, c->stream, &c->retired_tables), "twiddle tables");
   nn_transform xa, xb;
   nn_status st = xform_reserve(c, &xa, s);
   if (st != NN_OK) return st;
@@ -718,7 +722,7 @@ nn_status batch_plan(nn_context* c, nn_batch* B, const u64* na, const u64* nb, c
     return NN_ERR_INVALID;
   }
   B->smem = smem;
-  NN_CK(c, nn::tables_ensure(c->tables, max_s, c->stream), "twiddle tables");
+  NN_CK(c, nn::tables_ensure(c->tables, max_s, c->stream, &c->retired_tables), "twiddle tables");
   int per_sm = 0;
   NN_CK(c, nn::batch_configure(&per_sm, smem), "batch kernel attributes");
   if (c->batch_blocks_per_sm > 0) per_sm = std::min(per_sm, c->batch_blocks_per_sm);
@@ -932,6 +936,8 @@ nn_status nn_context_destroy(nn_context* c) {
   for (int i = 0; i < 3; ++i) dev_free(c, c->scratch[i], c->scratch_words[i]);
   cudaStreamSynchronize(c->own);
   nn::tables_free(c->tables);
+  for (u64* p : c->retired_tables) cudaFree(p);
+  c->retired_tables.clear();
   nn::scan_free(c->scan);
   c->stage.release();
   cudaStreamSynchronize(c->copy);

@@ -29,7 +29,11 @@ struct Tables {
   int scale = 0;
   u32* err = nullptr;    // device error word for kernels whose bounded waits run out (the context's)
 };
-cudaError_t tables_ensure(Tables& t, int s, cudaStream_t st);
+// Grows the tables to scale s on stream st.  The tables they replace are
+// handed to `retired` when given (freed by the caller once no stream can
+// still read them: kernels on other streams may hold their pointers), else
+// freed in stream order on st.
+cudaError_t tables_ensure(Tables& t, int s, cudaStream_t st, std::vector<u64*>* retired = nullptr);
 void tables_free(Tables& t);
 
 // One tiled pass over transform levels [lambda0, lambda0 + R) with C columns per tile.

@@ -553,7 +553,7 @@ cudaError_t upload_primes() {
   return e == cudaSuccess ? upload_primes_batch(ps) : e;
 }
 
-cudaError_t tables_ensure(Tables& t, int s, cudaStream_t st) {
+cudaError_t tables_ensure(Tables& t, int s, cudaStream_t st, std::vector<u64*>* retired) {
   if (s < 2) s = 2;
   const u64 need = 1ull << (s - 1);
   if (t.cap >= need) return cudaSuccess;
@@ -596,8 +596,13 @@ cudaError_t tables_ensure(Tables& t, int s, cudaStream_t st) {
     }
   }
   e = cudaGetLastError();
-  if (t.root) cudaFreeAsync(t.root, st);
-  if (t.iroot) cudaFreeAsync(t.iroot, st);
+  for (u64* old : {t.root, t.iroot}) {
+    if (!old) continue;
+    if (retired)
+      retired->push_back(old);
+    else
+      cudaFreeAsync(old, st);
+  }
   t.root = root;
   t.iroot = iroot;
   t.cap = need;

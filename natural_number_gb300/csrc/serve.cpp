@@ -360,6 +360,10 @@ nn_status nn_server_create(int device, uint64_t hbm_budget, int streams, int div
     delete S;
     return st;
   }
+  // Every product stays inside its batch's kernel: batches run on several
+  // streams at once, and a product run on its own (the batch_solo_scale
+  // route) would use the context's one carry-scan scratch from each of them.
+  nn_context_set_tunable(S->ctx, "batch_solo_scale", 0);
   // Product batches run on high-priority streams and divisions (long chains
   // of dependent kernels on the worker contexts) on low-priority ones, so a
   // batch that arrives while a division runs gets the SMs as they free up.

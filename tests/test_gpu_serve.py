@@ -66,3 +66,28 @@ def test_budget_admission_and_rejection(oracle):
         srv.submit_mul(np.ones(1 << 22, dtype=np.uint64), np.ones(1 << 22, dtype=np.uint64))
     assert e.value.status == nn.NN_ERR_BUDGET
     srv.close()
+
+
+def test_served_large_products_on_concurrent_streams():
+    """Products of 2^21 limbs and more (scale 22 and up), several batches in
+    flight on the server's streams at once, the twiddle tables growing while
+    earlier batches run: every product equals the one computed on a plain
+    context."""
+    import natural_number_gb300 as nn
+    sizes = [(1 << 21, 1 << 21), (300, 200), ((1 << 21) + 7, (1 << 21) - 3), (5000, 7000), ((1 << 22) - 5, 1 << 21),
+             (1 << 20, (1 << 20) + 1), ((1 << 21) + 1, 4000), (1 << 21, (1 << 21) + 9)]
+    pairs = [(limbs(700 + k, x), limbs(800 + k, y)) for k, (x, y) in enumerate(sizes)]
+    srv = nn.Server(0, hbm_budget=0, streams=3, div_workers=1)
+    ctx = nn.Context(0)
+    try:
+        for rnd in range(2):
+            tickets = []
+            for a, b in pairs:
+                tickets.append(srv.submit_mul(a, b))
+                time.sleep(0.001)
+            for t, (a, b) in zip(tickets, pairs):
+                got = srv.wait(t, 120.0)[0]
+                assert np.array_equal(_norm(got), _norm(ctx.mul(a, b))), (rnd, a.size, b.size)
+    finally:
+        srv.close()
+        ctx.close()
