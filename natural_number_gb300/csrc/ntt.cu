@@ -596,6 +596,10 @@ cudaError_t tables_ensure(Tables& t, int s, cudaStream_t st, std::vector<u64*>* 
     }
   }
   e = cudaGetLastError();
+  // The new tables are built on `st`, but kernels on other streams of the
+  // same context (a server's concurrent batches, a caller's set_stream) read
+  // them from the next launch on: finish building before they are handed out.
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   for (u64* old : {t.root, t.iroot}) {
     if (!old) continue;
     if (retired)
