@@ -19,6 +19,7 @@
 
 #include "../../include/natural_gb300.h"
 #include "nn_internal.h"
+#include "stage_ring.h"
 
 using nn::u64;
 
@@ -36,91 +37,67 @@ int ntt_scale(u64 n1, u64 n2) {  // get_NTT_scale (natural.h:384-386)
 // the stream's earlier work before it returns, which would stop the host
 // from planning the next batch while the GPU runs this one; from this ring
 // the copy is queued and the call returns at once.  Regions are handed out
-// in order; one is reused after the event recorded behind its copy.
-struct Stager {
-  struct Region {
-    u64 off, len;
-    cudaEvent_t done;
-  };
-  char* base = nullptr;
-  u64 cap = 0, head = 0;
-  std::vector<Region> live;  // oldest first
+// in order; one is reused after the event recorded behind its copy (the
+// bookkeeping: RegionRing, stage_ring.h).
+struct CudaEvents {
+  using event = cudaEvent_t;
   std::vector<cudaEvent_t> spare;
+  bool done(cudaEvent_t e) { return cudaEventQuery(e) == cudaSuccess; }
+  void wait(cudaEvent_t e) { cudaEventSynchronize(e); }
+  void recycle(cudaEvent_t e) { spare.push_back(e); }
+};
 
-  void retire_front() {
-    spare.push_back(live.front().done);
-    live.erase(live.begin());
-  }
-  // Room for n bytes (256-byte granules), waiting for the copies that still
-  // read it; nullptr if no page-locked memory can be had.
-  char* reserve(u64 n) {
-    n = (n + 255) & ~255ull;
-    if (n > cap) {
-      while (!live.empty()) {
-        cudaEventSynchronize(live.front().done);
-        retire_front();
-      }
-      if (base) nn_host_free(base, cap);
-      cap = std::max<u64>(std::bit_ceil(2 * n), 16ull << 20);
-      base = static_cast<char*>(nn_host_alloc(cap));
-      head = 0;
-      if (!base) {
-        cap = 0;
-        return nullptr;
-      }
-    }
-    u64 off = head + n <= cap ? head : 0;
-    for (;;) {
-      while (!live.empty() && cudaEventQuery(live.front().done) == cudaSuccess) retire_front();
-      bool overlap = false;
-      for (const Region& r : live) overlap = overlap || (r.off < off + n && off < r.off + r.len);
-      if (!overlap) break;
-      cudaEventSynchronize(live.front().done);
-      retire_front();
-    }
-    head = off + n;
-    live.push_back(Region{off, n, nullptr});
-    return base + off;
-  }
+struct Stager {
+  char* base = nullptr;
+  CudaEvents ev;
+  nn::RegionRing<CudaEvents> ring;
+
   // bytes from host memory at src to device memory at dst, queued on st.
   cudaError_t upload(void* dst, const void* src, u64 bytes, cudaStream_t st) {
     if (!bytes) return cudaSuccess;
-    char* h = reserve(bytes);
-    if (!h) return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);  // no page-locked memory
+    const u64 n = ring.granule(bytes);
+    if (n > ring.cap) {  // a larger ring, once every copy from this one is done
+      ring.drain(ev);
+      if (base) nn_host_free(base, ring.cap);
+      ring.cap = std::max<u64>(std::bit_ceil(2 * n), 16ull << 20);
+      ring.head = 0;
+      base = static_cast<char*>(nn_host_alloc(ring.cap));
+      if (!base) {  // no page-locked memory to be had
+        ring.cap = 0;
+        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
+      }
+    }
+    char* h = base + ring.place(n, ev);
     std::memcpy(h, src, bytes);
     cudaError_t e = cudaMemcpyAsync(dst, h, bytes, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) {
-      live.pop_back();
+      ring.drop();
       return e;
     }
-    if (spare.empty()) {
-      cudaEvent_t ev = nullptr;
-      e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
-      if (e == cudaSuccess) spare.push_back(ev);
+    cudaEvent_t done = nullptr;
+    if (!ev.spare.empty()) {
+      done = ev.spare.back();
+      ev.spare.pop_back();
+    } else {
+      e = cudaEventCreateWithFlags(&done, cudaEventDisableTiming);
     }
-    if (e == cudaSuccess) {
-      live.back().done = spare.back();
-      spare.pop_back();
-      e = cudaEventRecord(live.back().done, st);
-      if (e != cudaSuccess) spare.push_back(live.back().done);
-    }
+    if (e == cudaSuccess) e = cudaEventRecord(done, st);
     if (e != cudaSuccess) {  // the copy is queued but no event marks its end: wait for it here
+      if (done) ev.spare.push_back(done);
       cudaStreamSynchronize(st);
-      live.pop_back();
+      ring.drop();
+      return e;
     }
-    return e;
+    ring.seal(done);
+    return cudaSuccess;
   }
   void release() {
-    for (Region& r : live) {
-      cudaEventSynchronize(r.done);
-      cudaEventDestroy(r.done);
-    }
-    for (cudaEvent_t e : spare) cudaEventDestroy(e);
-    live.clear();
-    spare.clear();
-    if (base) nn_host_free(base, cap);
+    ring.drain(ev);
+    for (cudaEvent_t e : ev.spare) cudaEventDestroy(e);
+    ev.spare.clear();
+    if (base) nn_host_free(base, ring.cap);
     base = nullptr;
-    cap = head = 0;
+    ring.cap = ring.head = 0;
   }
 };
 }  // namespace
